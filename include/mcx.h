@@ -1,0 +1,233 @@
+/*
+ * mcx.h -- C ABI of the GB300 Metropolis engine for the McLiCS nematic
+ * lattice model (Lebwohl-Lasher / GHRL pair energies, electric field,
+ * bulk / slab / sphere / custom geometries with surface anchoring).
+ *
+ * Plain C types only: pointers, sizes, enums.  Directors cross the boundary
+ * in the reference's AoS layout ni[(i + Nx*(j + Ny*k))*3 + c]
+ * (include/define.h:10-12 of the reference); the engine keeps them on the
+ * GPU in a split red/black SoA layout and converts at the boundary.
+ *
+ * What each entry point replaces in the reference (paths relative to the
+ * McLiCS project root):
+ *
+ *   mcx_create        EvolveNGPU construction + one-time device setup:
+ *                     simulator::Setup_simmulation (src/simulatorGPU.cpp:24-108),
+ *                     thermalEvolveNGPU::run device allocation/copies and
+ *                     initRNG (src/evolve_thermal.cu:44-64), setGPUup/
+ *                     setSurfaces/passGPUns (src/evolve.cu:205-263,275-341),
+ *                     setGHRL (src/io.cpp:277-302).  Replaces the
+ *                     one-lattice-per-process statics with a batch of
+ *                     replicas of any sizes.
+ *   mcx_set_state     cudaMemcpy(d_ni, ni, ...) (src/evolve_thermal.cu:58)
+ *   mcx_get_state     cudaMemcpy(ni, d_ni, ...) (src/evolve_thermal.cu:90,96)
+ *   mcx_set_mask      Geometry::set_point_type_normals for custom geometry
+ *                     (src/geometry_custom.cpp:57-128) and the pt/ns uploads
+ *                     (src/evolve_thermal.cu:59, src/evolve.cu:321-325)
+ *   mcx_set_temperature  cudaMemcpy(d_T, &params->T, ...) (src/evolve_thermal.cu:80)
+ *   mcx_set_field     params->elecE stepping (src/evolve_electric.cpp:59)
+ *   mcx_sweep         EvolveNGPU::Monte_Carlo_Step_GPU (src/evolve.cu:265-388)
+ *                     / EvolveN::Monte_Carlo_Step (src/evolve.cpp:64-179),
+ *                     n times, with the step-size rule applied on the GPU;
+ *                     with measure != 0 also energy_calculator_GPU
+ *                     (src/evolve.cu:390-436) + Matrice_constructor +
+ *                     Eigen_value_evaluation (src/parameter_order.cpp:11-60)
+ *                     after every sweep, accumulated as the run loops do
+ *                     (src/evolve_thermal.cpp:66-79).
+ *   mcx_measure       one energy_calculator + Matrice_constructor +
+ *                     Eigen_value_evaluation on the current state.
+ *   mcx_get_stats     the S1/S2/E/E2 means written to po.dat
+ *                     (src/evolve_thermal.cpp:80-87).
+ *   mcx_run_file      ./mc_sim <paramfile> (src/main.cpp:63-83) with
+ *                     evol thermalGPU / electricGPU / stepGPU / quenchGPU
+ *                     (also accepted: thermalGB300 etc.).
+ *
+ * Errors are returned as status codes (the reference calls exit(n)); the
+ * message of the last failure is available from mcx_last_error().  An engine
+ * handle is single-threaded and owns one CUDA stream; every call that returns
+ * host data synchronises that stream.
+ */
+#ifndef MCX_H_
+#define MCX_H_
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MCX_MAX_SURFACES 16
+#define MCX_MEASURE_LEN 16
+#define MCX_STATS_LEN 16
+
+typedef enum {
+  MCX_OK = 0,
+  MCX_ERR_INVALID = 1,     /* bad argument (sizes, enums, replica index) */
+  MCX_ERR_CUDA = 2,        /* a CUDA call failed; see mcx_last_error */
+  MCX_ERR_NOMEM = 3,       /* device or host allocation failed */
+  MCX_ERR_UNSUPPORTED = 4, /* a configuration the engine does not run */
+  MCX_ERR_IO = 5,          /* file could not be read or written */
+  MCX_ERR_PARSE = 6        /* parameter or geometry file is malformed */
+} mcx_status;
+
+typedef enum { MCX_POT_LL = 0, MCX_POT_GHRL = 1 } mcx_potential;
+typedef enum { MCX_GEO_BULK = 0, MCX_GEO_SLAB = 1, MCX_GEO_SPHERE = 2, MCX_GEO_CUSTOM = 3 } mcx_geometry;
+typedef enum { MCX_BOUND_FREE = 0, MCX_BOUND_PERIODIC = 1 } mcx_bound;
+typedef enum {
+  MCX_ANCH_HOMEOTROPIC = 0,      /* -W (n.s)^2, s = surface normal */
+  MCX_ANCH_FG = 1,               /* +W (n.s)^2 (planar) */
+  MCX_ANCH_RP = 2,               /* -W (n.d)^2, d from (theta_s, phi_s) */
+  MCX_ANCH_STRONG = 3,           /* -W (n.d)^2 */
+  MCX_ANCH_HOMEOTROPIC_GHRL = 4, /* W * GHRL bond form against s */
+  MCX_ANCH_FG_GHRL = 5,
+  MCX_ANCH_RP_GHRL = 6,
+  MCX_ANCH_STRONG_GHRL = 7
+} mcx_anchoring;
+
+/* One replica: a lattice, its physics and its Monte Carlo state.  Field
+ * names follow the reference's parameter keys (include/parameters.h:11-83). */
+typedef struct {
+  int nx, ny, nz;
+  int geometry;                /* mcx_geometry */
+  int xbound, ybound, zbound;  /* mcx_bound; slab forces z free, sphere all free */
+  int potential;               /* mcx_potential */
+  float A;                     /* LL coupling */
+  float k11, k22, k33, p0;     /* GHRL elastic constants and pitch (0 = achiral) */
+  float elecA;                 /* dielectric anisotropy; 0 disables the field term */
+  float elecX, elecY, elecZ;   /* field direction (not normalised, as in the reference) */
+  float elecE;                 /* field strength */
+  float T;                     /* temperature */
+  float ang_var;               /* initial step size (the reference starts at 0.5) */
+  unsigned int seed;           /* Philox key word 0 */
+  unsigned int stream;         /* Philox key word 1; distinct per replica */
+  int n_surfaces;
+  int anchoring[MCX_MAX_SURFACES]; /* mcx_anchoring, per surface id (pt - 2) */
+  float W[MCX_MAX_SURFACES];
+  float theta_s[MCX_MAX_SURFACES]; /* degrees */
+  float phi_s[MCX_MAX_SURFACES];   /* degrees */
+  float radius;                /* sphere: droplet radius; 0 = Nz/2 as the reference */
+} mcx_replica_desc;
+
+typedef struct mcx_engine mcx_engine;
+
+/* mcx_measure() output layout (MCX_MEASURE_LEN doubles). */
+enum {
+  MCX_M_E = 0,        /* energy per site over all sites, the CPU path's E (src/evolve.cpp:27-62) */
+  MCX_M_E_VALID = 1,  /* energy per active site (the GPU path's normalisation) */
+  MCX_M_Q = 2,        /* 9 entries, row-major Q-tensor */
+  MCX_M_S = 11,       /* largest eigenvalue of Q */
+  MCX_M_DIRECTOR = 12,/* 3 entries: its unit eigenvector */
+  MCX_M_VALID = 15    /* number of active sites */
+};
+
+/* mcx_get_stats() output layout (MCX_STATS_LEN doubles), sums over measured
+ * sweeps since the last reset. */
+enum {
+  MCX_ST_N = 0,        /* measured sweeps */
+  MCX_ST_S1 = 1,       /* sum S */
+  MCX_ST_S2 = 2,       /* sum S^2 */
+  MCX_ST_E1 = 3,       /* sum E (all-site normalisation) */
+  MCX_ST_E2 = 4,       /* sum E^2 */
+  MCX_ST_EV1 = 5,      /* sum E_valid */
+  MCX_ST_EV2 = 6,      /* sum E_valid^2 */
+  MCX_ST_ACC = 7,      /* accepted moves, all sweeps since reset */
+  MCX_ST_SWEEPS = 8,   /* sweeps since reset */
+  MCX_ST_LAST_E = 9,   /* last measured E */
+  MCX_ST_LAST_S = 10,  /* last measured S */
+  MCX_ST_ANG_VAR = 11, /* current step size */
+  MCX_ST_SWEEP_INDEX = 12 /* total sweeps done (the RNG counter) */
+};
+
+int mcx_version(void);
+
+/* Allocates the device state for n_replicas replicas (each any size with even
+ * nx; periodic y/z need even ny/nz) and fills the geometry masks of
+ * bulk/slab/sphere replicas.  Directors start along +z; use mcx_set_state or
+ * mcx_init_random / mcx_init_homogeneous to set them. */
+mcx_status mcx_create(int n_replicas, const mcx_replica_desc *descs, mcx_engine **out);
+void mcx_destroy(mcx_engine *eng);
+/* Message of the last failure on this engine (eng == NULL: of the last
+ * failed mcx_create / mcx_run_file). */
+const char *mcx_last_error(const mcx_engine *eng);
+
+int mcx_num_replicas(const mcx_engine *eng);
+/* Copies a replica's descriptor as the engine uses it (bounds forced by the
+ * geometry, GHRL constants derived). ghrl_out (5 floats: lambda, mu, nu, rho,
+ * sigma) may be NULL. */
+mcx_status mcx_get_desc(const mcx_engine *eng, int replica, mcx_replica_desc *desc, float *ghrl_out);
+
+mcx_status mcx_set_state(mcx_engine *eng, int replica, const float *ni_aos);
+mcx_status mcx_get_state(mcx_engine *eng, int replica, float *ni_aos);
+/* Random directors uniform on the sphere (Philox keyed by seed, replica) and
+ * (0,0,1) on inactive sites (src/ic.cpp:27-59); homogeneous along
+ * (theta_0, phi_0) in degrees (src/ic.cpp:61-86). */
+mcx_status mcx_init_random(mcx_engine *eng, int replica, unsigned int seed);
+mcx_status mcx_init_homogeneous(mcx_engine *eng, int replica, float theta_0, float phi_0);
+
+/* pt: int per site (0 inactive, 1 bulk, >= 2 surface id + 2); ns_aos: surface
+ * normal per site (may be NULL: zeros). */
+mcx_status mcx_set_mask(mcx_engine *eng, int replica, const int *pt, const float *ns_aos);
+mcx_status mcx_get_mask(mcx_engine *eng, int replica, int *pt, float *ns_aos);
+
+/* replica = -1 applies to every replica. */
+mcx_status mcx_set_temperature(mcx_engine *eng, int replica, float T);
+mcx_status mcx_set_field(mcx_engine *eng, int replica, float elecE);
+mcx_status mcx_set_step(mcx_engine *eng, int replica, float ang_var);
+
+/* n_sweeps red/black Metropolis sweeps of every replica, on the engine's
+ * stream (asynchronous).  measure != 0 measures E, Q and S after every sweep
+ * and adds them to the running sums read by mcx_get_stats. */
+mcx_status mcx_sweep(mcx_engine *eng, int n_sweeps, int measure);
+mcx_status mcx_sync(mcx_engine *eng);
+mcx_status mcx_measure(mcx_engine *eng, int replica, double *out /* MCX_MEASURE_LEN */);
+mcx_status mcx_get_stats(mcx_engine *eng, int replica, double *out /* MCX_STATS_LEN */);
+mcx_status mcx_reset_stats(mcx_engine *eng, int replica);
+
+/* Records E and S of every measured sweep of every replica in a device ring
+ * of `capacity` sweeps (0 disables); mcx_get_series copies the last `count`
+ * values (E then S interleaved per sweep) of one replica. */
+mcx_status mcx_set_series(mcx_engine *eng, int capacity);
+mcx_status mcx_get_series(mcx_engine *eng, int replica, int count, double *es_out);
+
+/* One red/black pass (colour 0 or 1) of one replica with a trace: per site
+ * (AoS order) the float energy change, the decision and the proposed
+ * director.  Sites not updated in the pass get dE = 0, acc = 255.  Used by
+ * the parity tests; does not advance the RNG counter or the step size. */
+mcx_status mcx_debug_pass(mcx_engine *eng, int replica, int colour, float *dE, unsigned char *acc,
+                          float *proposal_aos);
+
+/* Kernel launches issued by this engine since creation (sweep, measure and
+ * epilogue kernels; graph launches count each kernel node). */
+long long mcx_kernel_launches(const mcx_engine *eng);
+
+/* The engine's CUDA stream (a cudaStream_t), for callers that record events
+ * or order their own work against the engine's. */
+void *mcx_stream(mcx_engine *eng);
+
+/* n_sweeps unmeasured sweeps launched one kernel at a time with CUDA events
+ * around every red/black pass kernel; pass_ms receives the summed duration of
+ * the 2*n_sweeps pass kernels, total_ms the whole sequence.  For profiling:
+ * the sweeps are real (state, RNG counter and step size advance). */
+mcx_status mcx_pass_timing(mcx_engine *eng, int n_sweeps, float *pass_ms, float *total_ms);
+
+/* Host-only helpers (no GPU needed). */
+/* setGHRL (src/io.cpp:277-302): out = lambda, mu, nu, rho, sigma. */
+void mcx_ghrl_constants(float k11, float k22, float k33, float p0, float *out5);
+/* Geometry::set_point_type_normals of bulk / slab / sphere
+ * (src/geometry_bulk.cpp:57-61, src/geometry_slab.cpp:47-67,
+ * src/geometry_sphere.cpp:28-54) in AoS order; MCX_ERR_INVALID for custom. */
+mcx_status mcx_build_mask(const mcx_replica_desc *desc, int *pt, float *ns_aos);
+/* Custom geometry file (src/geometry_custom.cpp:57-128) for an nx*ny*nz
+ * lattice; *n_surfaces receives max(pt) - 1. */
+mcx_status mcx_read_geometry(const char *path, int nx, int ny, int nz, int *pt, float *ns_aos, int *n_surfaces);
+/* Parses and validates a parameter file (src/io.cpp:81-253) without running
+ * it; desc (may be NULL) receives replica 0's descriptor. */
+mcx_status mcx_check_file(const char *param_file, mcx_replica_desc *desc);
+
+/* ./mc_sim <param_file> (src/main.cpp:63-83): reads the reference's parameter
+ * file (src/io.cpp:81-253), runs the selected mode on the GPU and writes
+ * po.dat and director_field_*.csv into out_dir (NULL: current directory). */
+mcx_status mcx_run_file(const char *param_file, const char *out_dir);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,191 @@
+// mcx_device.cuh -- device-side building blocks of the GB300 Metropolis
+// engine: replica table, Philox4x32-10, pair / anchoring / field energies.
+//
+// Director layout in HBM (per replica): a split red/black SoA.  Colour
+// c = (i + j + k) & 1; colour c of row (j, k) holds the sites
+// i = 2h + ((c + j + k) & 1), h = 0 .. hx-1 (hx = nx/2), stored at
+//   dir[dir_off + (c*3 + comp)*plane + (j + ny*k)*hs + h],
+// hs = hx rounded up to a multiple of 4 (16-byte rows), plane = hs*ny*nz.
+// A red/black pass reads the whole other colour and reads + writes its own,
+// each as coalesced float4 rows.  Point types (pt) use the same split layout
+// as bytes; surface normals (ns) as floats.
+#pragma once
+#include <cstdint>
+
+namespace mcx {
+
+constexpr int kMaxSurf = 16;
+constexpr int kBlock = 128;  // threads per CTA of the sweep / measure kernels
+
+enum : int { POT_LL = 0, POT_GHRL = 1 };
+enum : int { BOUND_FREE = 0, BOUND_PERIODIC = 1 };
+enum : int {
+  ANCH_HOMEOTROPIC = 0,
+  ANCH_FG = 1,
+  ANCH_RP = 2,
+  ANCH_STRONG = 3,
+  ANCH_HOMEOTROPIC_GHRL = 4,
+  ANCH_FG_GHRL = 5,
+  ANCH_RP_GHRL = 6,
+  ANCH_STRONG_GHRL = 7
+};
+// Philox counter word 3: which stream of uniforms.
+enum : uint32_t { TAG_PLAIN = 0u, TAG_VMF = 1u, TAG_IC = 0x1C000000u };
+
+// Per-replica constants, resident in device memory (read-only in kernels).
+struct RepDev {
+  int nx, ny, nz;
+  int hx, hs, g4;  // half-row length, padded stride, float4 groups per row
+  int xb, yb, zb;
+  int nsurf;
+  int valid;  // active sites
+  int ntot;   // nx*ny*nz
+  int pad0;
+  long long plane;    // elements per (colour, component) plane
+  long long dir_off;  // float offset of this replica's [2][3][plane] block
+  long long pt_off;   // byte offset of its [2][plane] point types
+  long long ns_off;   // float offset of its [2][3][plane] normals
+  long long ngroups;  // float4 groups per colour = g4*ny*nz
+  float A, elecA, elecE, ex, ey, ez;
+  float lam, mu, nu, rho, sigma;
+  uint32_t seed, stream;
+  int anch[kMaxSurf];
+  float W[kMaxSurf];
+  float dx[kMaxSurf], dy[kMaxSurf], dz[kMaxSurf];  // anchoring easy axis
+};
+
+// Mutable per-replica scalars, one struct per replica in device memory.
+struct RepState {
+  float T;
+  float ang_var;
+  unsigned int acc;          // accepted moves of the sweep in progress
+  unsigned int pad;
+  unsigned long long sweep;  // RNG counter: sweeps done
+};
+
+// Running sums (doubles), indexed by the MCX_ST_* layout of mcx.h.
+constexpr int kStats = 16;
+// Measurement accumulators: E_all, E_valid, then sum n_a n_b for
+// xx, xy, xz, yy, yz, zz.
+constexpr int kMacc = 8;
+
+// ---------------------------------------------------------------------------
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11).
+// ---------------------------------------------------------------------------
+__host__ __device__ __forceinline__ void mulhilo32(uint32_t a, uint32_t b, uint32_t &hi, uint32_t &lo) {
+#ifdef __CUDA_ARCH__
+  lo = a * b;
+  hi = __umulhi(a, b);
+#else
+  uint64_t p = (uint64_t)a * b;
+  hi = (uint32_t)(p >> 32);
+  lo = (uint32_t)p;
+#endif
+}
+
+__host__ __device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint32_t k0, uint32_t k1) {
+#pragma unroll
+  for (int r = 0; r < 10; r++) {
+    uint32_t hi0, lo0, hi1, lo1;
+    mulhilo32(0xD2511F53u, c.x, hi0, lo0);
+    mulhilo32(0xCD9E8D57u, c.z, hi1, lo1);
+    c = make_uint4(hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0);
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+  return c;
+}
+
+// 24-bit uniform on [0, 1), exact in float.
+__host__ __device__ __forceinline__ float u01(uint32_t x) { return (float)(x >> 8) * 5.9604644775390625e-8f; }
+
+// ---------------------------------------------------------------------------
+// Energies.  Neighbour slots follow the reference order x+, x-, y+, y-, z+,
+// z- (src/geometry.cpp:19-72); slot d has axis d >> 1 and sign +1 for even d.
+// ---------------------------------------------------------------------------
+
+// Chiral term component as the reference writes it (src/potential.cpp:30-32)
+// for r = +e_axis: (a x b) with the reference's sign convention.
+template <int AXIS>
+__device__ __forceinline__ float cross_ref(float ax, float ay, float az, float bx, float by, float bz) {
+  if (AXIS == 0) return az * by - ay * bz;
+  if (AXIS == 1) return ax * bz - az * bx;
+  return ay * bx - ax * by;
+}
+
+// GHRL bond energy (src/potential.cpp:22-38) for r = sign * e_axis.
+template <int AXIS>
+__device__ __forceinline__ float ghrl_bond(const RepDev &R, float ax, float ay, float az, float bx, float by, float bz,
+                                           float sign) {
+  const float ai = AXIS == 0 ? ax : (AXIS == 1 ? ay : az);
+  const float aj = AXIS == 0 ? bx : (AXIS == 1 ? by : bz);
+  const float nij = ax * bx + ay * by + az * bz;
+  const float P2 = 1.5f * nij * nij - 0.5f;
+  const float E1 = 1.5f * ai * ai + 1.5f * aj * aj - 1.0f;
+  const float cr = sign * cross_ref<AXIS>(ax, ay, az, bx, by, bz);
+  const float sg = nij > 0.f ? 1.f : -1.f;
+  return E1 * (R.rho * P2 + R.lam) + R.mu * (ai * aj * nij - (1.0f / 9.0f)) + R.nu * P2 + R.sigma * sg * cr;
+}
+
+// Anchoring energy of surface `sid` (src/anchoring_*.cpp, CPU semantics).
+__device__ __forceinline__ float ghrl_form(const RepDev &R, float ai, float aj, float nij, float cross) {
+  const float P2 = 1.5f * nij * nij - 0.5f;
+  const float E1 = 1.5f * ai * ai + 1.5f * aj * aj - 1.0f;
+  const float sg = nij > 0.f ? 1.f : -1.f;
+  return E1 * (R.rho * P2 + R.lam) + R.mu * (ai * aj * nij) + R.nu * P2 + R.sigma * sg * cross;
+}
+
+__device__ __forceinline__ float cross3(float ax, float ay, float az, float bx, float by, float bz, float rx, float ry,
+                                        float rz) {
+  return (az * by - ay * bz) * rx + (ax * bz - az * bx) * ry + (ay * bx - ax * by) * rz;
+}
+
+static __device__ __noinline__ float surface_energy(const RepDev &R, int sid, float nx, float ny, float nz, float sx, float sy,
+                                             float sz) {
+  const float W = R.W[sid];
+  const float dx = R.dx[sid], dy = R.dy[sid], dz = R.dz[sid];
+  switch (R.anch[sid]) {
+    case ANCH_HOMEOTROPIC: {
+      const float c = nx * sx + ny * sy + nz * sz;
+      return -W * c * c;
+    }
+    case ANCH_FG: {
+      const float c = nx * sx + ny * sy + nz * sz;
+      return W * c * c;
+    }
+    case ANCH_RP:
+    case ANCH_STRONG:
+    case ANCH_STRONG_GHRL: {
+      const float c = nx * dx + ny * dy + nz * dz;
+      return -W * c * c;
+    }
+    case ANCH_HOMEOTROPIC_GHRL: {
+      const float a = nx * sx + ny * sy + nz * sz;
+      return W * ghrl_form(R, a, 1.0f, a, cross3(nx, ny, nz, sx, sy, sz, sx, sy, sz));
+    }
+    case ANCH_FG_GHRL: {
+      const float m = sqrtf(fabsf(nx * sx + ny * sy + nz * sz));
+      float vx = nx - sx * m, vy = ny - sy * m, vz = nz - sz * m;
+      const float L = sqrtf(fabsf(vx * vx + vy * vy + vz * vz));
+      const float d = L > 0.f ? L : 1.f;
+      vx /= d;
+      vy /= d;
+      vz /= d;
+      return W * ghrl_form(R, nx * sx + ny * sy + nz * sz, vx * sx + vy * sy + vz * sz, nx * vx + ny * vy + nz * vz,
+                           cross3(nx, ny, nz, vx, vy, vz, sx, sy, sz));
+    }
+    case ANCH_RP_GHRL:
+      return W * ghrl_form(R, nx * sx + ny * sy + nz * sz, dx * sx + dy * sy + dz * sz, nx * dx + ny * dy + nz * dz,
+                           cross3(nx, ny, nz, dx, dy, dz, sx, sy, sz));
+    default:
+      return 0.f;
+  }
+}
+
+// Electric term (src/potential.cpp:39-43).
+__device__ __forceinline__ float field_energy(const RepDev &R, float nx, float ny, float nz) {
+  const float d = R.elecE * (nx * R.ex + ny * R.ey + nz * R.ez);
+  return -R.elecA * d * d;
+}
+
+}  // namespace mcx

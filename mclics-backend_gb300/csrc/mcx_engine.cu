@@ -1,0 +1,673 @@
+// mcx_engine.cu -- the C ABI of include/mcx.h: a batch of replicas resident
+// on one GB300, swept by the red/black kernels of mcx_kernels.cu, with the
+// per-sweep sequence (pass 0, pass 1, [measure], epilogue) captured once into
+// CUDA graphs of kChunk sweeps and replayed.
+#include <cuda_runtime.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <string>
+#include <vector>
+
+#include "../../include/mcx.h"
+#include "mcx_device.cuh"
+#include "mcx_host.h"
+#include "mcx_kernels.cuh"
+
+using namespace mcx;
+
+namespace {
+constexpr int kChunk = 16;  // sweeps per captured graph
+std::string g_last_error;
+}  // namespace
+
+void mcx::set_last_error(const char *msg) { g_last_error = msg ? msg : ""; }
+
+struct mcx_engine {
+  int nrep = 0;
+  std::vector<mcx_replica_desc> desc;
+  std::vector<RepDev> rep;
+  std::vector<int2> map;
+  Variant var{};
+  cudaStream_t stream = nullptr;
+  RepDev *d_rep = nullptr;
+  int2 *d_map = nullptr;
+  float *d_dir = nullptr;
+  uint8_t *d_pt = nullptr;
+  float *d_ns = nullptr;
+  RepState *d_st = nullptr;
+  double *d_macc = nullptr;
+  double *d_stats = nullptr;
+  double *d_series = nullptr;
+  double *d_mout = nullptr;
+  int series_cap = 0;
+  float *d_stage = nullptr;  // AoS staging, 3 * max sites floats
+  int *d_stage_pt = nullptr;
+  long long max_sites = 0;
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};  // [measure]
+  int graph_nodes[2] = {0, 0};
+  long long launches = 0;
+  std::string err;
+};
+
+static mcx_status fail(mcx_engine *e, mcx_status st, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  if (e) e->err = buf;
+  else g_last_error = buf;
+  return st;
+}
+
+#define CK(e, call)                                                                                   \
+  do {                                                                                                \
+    cudaError_t _r = (call);                                                                          \
+    if (_r != cudaSuccess) return fail(e, MCX_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(_r));      \
+  } while (0)
+
+#define CKL(e)                                                                                        \
+  do {                                                                                                \
+    cudaError_t _r = cudaGetLastError();                                                              \
+    if (_r != cudaSuccess) return fail(e, MCX_ERR_CUDA, "kernel launch: %s", cudaGetErrorString(_r)); \
+  } while (0)
+
+static long long align_up(long long x, long long a) { return (x + a - 1) / a * a; }
+
+extern "C" int mcx_version(void) { return 1; }
+
+extern "C" const char *mcx_last_error(const mcx_engine *e) { return e ? e->err.c_str() : g_last_error.c_str(); }
+
+extern "C" int mcx_num_replicas(const mcx_engine *e) { return e ? e->nrep : 0; }
+
+extern "C" long long mcx_kernel_launches(const mcx_engine *e) { return e ? e->launches : 0; }
+
+static void free_engine(mcx_engine *e) {
+  if (!e) return;
+  for (int m = 0; m < 2; m++)
+    if (e->graph[m]) cudaGraphExecDestroy(e->graph[m]);
+  cudaFree(e->d_rep);
+  cudaFree(e->d_map);
+  cudaFree(e->d_dir);
+  cudaFree(e->d_pt);
+  cudaFree(e->d_ns);
+  cudaFree(e->d_st);
+  cudaFree(e->d_macc);
+  cudaFree(e->d_stats);
+  cudaFree(e->d_series);
+  cudaFree(e->d_mout);
+  cudaFree(e->d_stage);
+  cudaFree(e->d_stage_pt);
+  if (e->stream) cudaStreamDestroy(e->stream);
+  delete e;
+}
+
+extern "C" void mcx_destroy(mcx_engine *e) { free_engine(e); }
+
+static mcx_status check_desc(const mcx_replica_desc &d, int r) {
+  if (d.nx < 2 || d.ny < 1 || d.nz < 1) return fail(nullptr, MCX_ERR_INVALID, "replica %d: lattice %dx%dx%d too small", r, d.nx, d.ny, d.nz);
+  if ((long long)d.nx * d.ny * d.nz >= (1LL << 31)) return fail(nullptr, MCX_ERR_INVALID, "replica %d: more than 2^31 sites", r);
+  if (d.nx % 2) return fail(nullptr, MCX_ERR_UNSUPPORTED, "replica %d: nx = %d must be even (red/black rows)", r, d.nx);
+  if (d.geometry < 0 || d.geometry > 3) return fail(nullptr, MCX_ERR_INVALID, "replica %d: bad geometry %d", r, d.geometry);
+  if (d.potential < 0 || d.potential > 1) return fail(nullptr, MCX_ERR_INVALID, "replica %d: bad potential %d", r, d.potential);
+  if (d.n_surfaces < 0 || d.n_surfaces > MCX_MAX_SURFACES) return fail(nullptr, MCX_ERR_INVALID, "replica %d: bad surface count %d", r, d.n_surfaces);
+  for (int s = 0; s < d.n_surfaces; s++)
+    if (d.anchoring[s] < 0 || d.anchoring[s] > 7) return fail(nullptr, MCX_ERR_INVALID, "replica %d: bad anchoring %d on surface %d", r, d.anchoring[s], s);
+  if (d.geometry == MCX_GEO_SLAB && d.n_surfaces < 2) return fail(nullptr, MCX_ERR_INVALID, "replica %d: slab geometry needs 2 surfaces", r);
+  if (d.geometry == MCX_GEO_SPHERE && d.n_surfaces < 1) return fail(nullptr, MCX_ERR_INVALID, "replica %d: sphere geometry needs 1 surface", r);
+  return MCX_OK;
+}
+
+// Bounds as the geometry forces them (src/geometry_slab.cpp:23,
+// src/geometry_sphere.cpp:19-21), then the red/black requirement: a periodic
+// axis of odd length would make a site its own-colour neighbour.
+static void effective_bounds(mcx_replica_desc &d) {
+  if (d.geometry == MCX_GEO_SLAB) d.zbound = MCX_BOUND_FREE;
+  if (d.geometry == MCX_GEO_SPHERE) d.xbound = d.ybound = d.zbound = MCX_BOUND_FREE;
+}
+
+extern "C" mcx_status mcx_create(int n, const mcx_replica_desc *descs, mcx_engine **out) {
+  if (!out || !descs || n <= 0) return fail(nullptr, MCX_ERR_INVALID, "mcx_create: need n > 0 descriptors and an output pointer");
+  *out = nullptr;
+  for (int r = 0; r < n; r++) {
+    mcx_status st = check_desc(descs[r], r);
+    if (st) return st;
+    if (descs[r].potential != descs[0].potential)
+      return fail(nullptr, MCX_ERR_UNSUPPORTED, "all replicas of one engine must use the same pair potential");
+    mcx_replica_desc d = descs[r];
+    effective_bounds(d);
+    if ((d.ybound == MCX_BOUND_PERIODIC && d.ny % 2) || (d.zbound == MCX_BOUND_PERIODIC && d.nz % 2))
+      return fail(nullptr, MCX_ERR_UNSUPPORTED, "replica %d: periodic y/z axes need even ny/nz for red/black sweeps", r);
+  }
+  mcx_engine *e = new mcx_engine();
+  e->nrep = n;
+  e->desc.assign(descs, descs + n);
+  e->var.pot = descs[0].potential;
+  e->var.mask = false;
+  e->var.field = false;
+  long long dir_total = 0, pt_total = 0;
+  e->rep.resize(n);
+  for (int r = 0; r < n; r++) {
+    mcx_replica_desc &d = e->desc[r];
+    effective_bounds(d);
+    RepDev &R = e->rep[r];
+    memset(&R, 0, sizeof R);
+    R.nx = d.nx;
+    R.ny = d.ny;
+    R.nz = d.nz;
+    R.hx = d.nx / 2;
+    R.hs = (int)align_up(R.hx, 4);
+    R.g4 = R.hs / 4;
+    R.xb = d.xbound;
+    R.yb = d.ybound;
+    R.zb = d.zbound;
+    R.nsurf = d.n_surfaces;
+    R.ntot = d.nx * d.ny * d.nz;
+    R.plane = (long long)R.hs * d.ny * d.nz;
+    R.ngroups = (long long)R.g4 * d.ny * d.nz;
+    R.dir_off = dir_total;
+    dir_total += align_up(6 * R.plane, 64);
+    R.pt_off = pt_total;
+    pt_total += align_up(2 * R.plane, 256);
+    R.A = d.A;
+    R.elecA = d.elecA;
+    R.elecE = d.elecE;
+    R.ex = d.elecX;
+    R.ey = d.elecY;
+    R.ez = d.elecZ;
+    float g[5] = {0, 0, 1, 0, 0};
+    if (d.potential == MCX_POT_GHRL) ghrl_constants(d.k11, d.k22, d.k33, d.p0, g);
+    R.lam = g[0];
+    R.mu = g[1];
+    R.nu = g[2];
+    R.rho = g[3];
+    R.sigma = g[4];
+    R.seed = d.seed;
+    R.stream = d.stream;
+    for (int s = 0; s < d.n_surfaces; s++) {
+      R.anch[s] = d.anchoring[s];
+      R.W[s] = d.W[s];
+      float ax[3];
+      anchoring_axis(d.theta_s[s], d.phi_s[s], ax);
+      R.dx[s] = ax[0];
+      R.dy[s] = ax[1];
+      R.dz[s] = ax[2];
+    }
+    if (d.geometry != MCX_GEO_BULK) e->var.mask = true;
+    if (d.elecA != 0.f) e->var.field = true;
+    e->max_sites = std::max(e->max_sites, (long long)R.ntot);
+    for (long long b = 0; b < R.ngroups; b += kBlock) e->map.push_back(make_int2(r, (int)b));
+  }
+  for (int r = 0; r < n; r++) e->rep[r].ns_off = e->var.mask ? e->rep[r].dir_off : -1;
+  mcx_status st = MCX_OK;
+#define CKC(call)                                                                                  \
+  do {                                                                                             \
+    cudaError_t _r = (call);                                                                       \
+    if (_r != cudaSuccess) {                                                                       \
+      st = fail(nullptr, _r == cudaErrorMemoryAllocation ? MCX_ERR_NOMEM : MCX_ERR_CUDA, "%s: %s", #call, \
+                cudaGetErrorString(_r));                                                           \
+      free_engine(e);                                                                              \
+      return st;                                                                                   \
+    }                                                                                              \
+  } while (0)
+  CKC(cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking));
+  CKC(cudaMalloc(&e->d_dir, sizeof(float) * dir_total));
+  CKC(cudaMemsetAsync(e->d_dir, 0, sizeof(float) * dir_total, e->stream));
+  if (e->var.mask) {
+    CKC(cudaMalloc(&e->d_pt, pt_total));
+    CKC(cudaMemsetAsync(e->d_pt, 0, pt_total, e->stream));
+    CKC(cudaMalloc(&e->d_ns, sizeof(float) * dir_total));
+    CKC(cudaMemsetAsync(e->d_ns, 0, sizeof(float) * dir_total, e->stream));
+  }
+  CKC(cudaMalloc(&e->d_rep, sizeof(RepDev) * n));
+  CKC(cudaMalloc(&e->d_map, sizeof(int2) * e->map.size()));
+  CKC(cudaMalloc(&e->d_st, sizeof(RepState) * n));
+  CKC(cudaMalloc(&e->d_macc, sizeof(double) * kMacc * n));
+  CKC(cudaMemsetAsync(e->d_macc, 0, sizeof(double) * kMacc * n, e->stream));
+  CKC(cudaMalloc(&e->d_stats, sizeof(double) * kStats * n));
+  CKC(cudaMemsetAsync(e->d_stats, 0, sizeof(double) * kStats * n, e->stream));
+  CKC(cudaMalloc(&e->d_mout, sizeof(double) * 16 * n));
+  CKC(cudaMalloc(&e->d_stage, sizeof(float) * 3 * e->max_sites));
+  CKC(cudaMalloc(&e->d_stage_pt, sizeof(int) * e->max_sites));
+  CKC(cudaMemcpyAsync(e->d_map, e->map.data(), sizeof(int2) * e->map.size(), cudaMemcpyHostToDevice, e->stream));
+  // masks: valid counts first (they go into RepDev)
+  std::vector<int> pt;
+  std::vector<float> ns;
+  for (int r = 0; r < n; r++) {
+    RepDev &R = e->rep[r];
+    build_mask(e->desc[r], pt, ns);  // custom geometry starts as all-bulk until mcx_set_mask
+    long v = 0;
+    for (int x : pt) v += x != 0;
+    R.valid = (int)v;
+  }
+  CKC(cudaMemcpyAsync(e->d_rep, e->rep.data(), sizeof(RepDev) * n, cudaMemcpyHostToDevice, e->stream));
+  std::vector<RepState> hs(n);
+  for (int r = 0; r < n; r++) {
+    hs[r].T = e->desc[r].T;
+    hs[r].ang_var = e->desc[r].ang_var > 0 ? e->desc[r].ang_var : 0.5f;
+    hs[r].acc = 0;
+    hs[r].pad = 0;
+    hs[r].sweep = 0;
+  }
+  CKC(cudaMemcpyAsync(e->d_st, hs.data(), sizeof(RepState) * n, cudaMemcpyHostToDevice, e->stream));
+  CKC(cudaStreamSynchronize(e->stream));
+  for (int r = 0; r < n; r++) {
+    if (e->var.mask) {
+      build_mask(e->desc[r], pt, ns);
+      st = mcx_set_mask(e, r, pt.data(), ns.data());
+      if (st) {
+        g_last_error = e->err;
+        free_engine(e);
+        return st;
+      }
+    }
+    st = mcx_init_homogeneous(e, r, 0.f, 0.f);
+    if (st) {
+      g_last_error = e->err;
+      free_engine(e);
+      return st;
+    }
+  }
+  CKC(cudaStreamSynchronize(e->stream));
+#undef CKC
+  *out = e;
+  return MCX_OK;
+}
+
+static mcx_status check_rep(mcx_engine *e, int r) {
+  if (!e) return fail(nullptr, MCX_ERR_INVALID, "null engine");
+  if (r < 0 || r >= e->nrep) return fail(e, MCX_ERR_INVALID, "replica %d out of range [0, %d)", r, e->nrep);
+  return MCX_OK;
+}
+
+extern "C" mcx_status mcx_get_desc(const mcx_engine *ce, int r, mcx_replica_desc *d, float *ghrl) {
+  mcx_engine *e = const_cast<mcx_engine *>(ce);
+  if (mcx_status st = check_rep(e, r)) return st;
+  if (d) *d = e->desc[r];
+  if (ghrl) {
+    const RepDev &R = e->rep[r];
+    ghrl[0] = R.lam;
+    ghrl[1] = R.mu;
+    ghrl[2] = R.nu;
+    ghrl[3] = R.rho;
+    ghrl[4] = R.sigma;
+  }
+  return MCX_OK;
+}
+
+extern "C" mcx_status mcx_set_state(mcx_engine *e, int r, const float *ni) {
+  if (mcx_status st = check_rep(e, r)) return st;
+  if (!ni) return fail(e, MCX_ERR_INVALID, "null director array");
+  const RepDev &R = e->rep[r];
+  CK(e, cudaMemcpyAsync(e->d_stage, ni, sizeof(float) * 3 * R.ntot, cudaMemcpyHostToDevice, e->stream));
+  launch_aos_to_split(R, e->d_stage, e->d_dir, e->stream);
+  CKL(e);
+  CK(e, cudaStreamSynchronize(e->stream));
+  return MCX_OK;
+}
+
+extern "C" mcx_status mcx_get_state(mcx_engine *e, int r, float *ni) {
+  if (mcx_status st = check_rep(e, r)) return st;
+  if (!ni) return fail(e, MCX_ERR_INVALID, "null director array");
+  const RepDev &R = e->rep[r];
+  launch_split_to_aos(R, e->d_dir, e->d_stage, e->stream);
+  CKL(e);
+  CK(e, cudaMemcpyAsync(ni, e->d_stage, sizeof(float) * 3 * R.ntot, cudaMemcpyDeviceToHost, e->stream));
+  CK(e, cudaStreamSynchronize(e->stream));
+  return MCX_OK;
+}
+
+extern "C" mcx_status mcx_init_random(mcx_engine *e, int r, unsigned int seed) {
+  if (mcx_status st = check_rep(e, r)) return st;
+  launch_init(e->rep[r], e->d_pt, e->d_dir, 0, seed, 0.f, 0.f, 1.f, e->stream);
+  CKL(e);
+  CK(e, cudaStreamSynchronize(e->stream));
+  return MCX_OK;
+}
+
+extern "C" mcx_status mcx_init_homogeneous(mcx_engine *e, int r, float theta_0, float phi_0) {
+  if (mcx_status st = check_rep(e, r)) return st;
+  // src/ic.cpp:77-79 (double math, stored as float)
+  const float fx = (float)(sin(theta_0 * M_PI / 180) * cos(phi_0 * M_PI / 180));
+  const float fy = (float)(sin(theta_0 * M_PI / 180) * sin(phi_0 * M_PI / 180));
+  const float fz = (float)cos(theta_0 * M_PI / 180);
+  launch_init(e->rep[r], e->d_pt, e->d_dir, 1, 0, fx, fy, fz, e->stream);
+  CKL(e);
+  CK(e, cudaStreamSynchronize(e->stream));
+  return MCX_OK;
+}
+
+extern "C" mcx_status mcx_set_mask(mcx_engine *e, int r, const int *pt, const float *ns) {
+  if (mcx_status st = check_rep(e, r)) return st;
+  if (!pt) return fail(e, MCX_ERR_INVALID, "null point-type array");
+  RepDev &R = e->rep[r];
+  long v = 0;
+  for (long s = 0; s < R.ntot; s++) {
+    if (pt[s] < 0 || pt[s] > 255) return fail(e, MCX_ERR_INVALID, "point type %d at site %ld out of [0, 255]", pt[s], s);
+    if (pt[s] > 1 && pt[s] - 2 >= R.nsurf)
+      return fail(e, MCX_ERR_INVALID, "point type %d at site %ld names surface %d but the replica has %d", pt[s], s, pt[s] - 2, R.nsurf);
+    v += pt[s] != 0;
+  }
+  if (!e->var.mask) {
+    bool all_bulk = true;
+    for (long s = 0; s < R.ntot && all_bulk; s++) all_bulk = pt[s] == 1;
+    if (all_bulk) return MCX_OK;
+    return fail(e, MCX_ERR_UNSUPPORTED, "engine was created without masks (all replicas bulk); create it with a non-bulk geometry");
+  }
+  if (v == 0) return fail(e, MCX_ERR_INVALID, "mask has no active site");
+  CK(e, cudaMemcpyAsync(e->d_stage_pt, pt, sizeof(int) * R.ntot, cudaMemcpyHostToDevice, e->stream));
+  if (ns) CK(e, cudaMemcpyAsync(e->d_stage, ns, sizeof(float) * 3 * R.ntot, cudaMemcpyHostToDevice, e->stream));
+  launch_mask_to_split(R, e->d_stage_pt, ns ? e->d_stage : nullptr, e->d_pt, e->d_ns, e->stream);
+  CKL(e);
+  R.valid = (int)v;
+  CK(e, cudaMemcpyAsync(&e->d_rep[r].valid, &R.valid, sizeof(int), cudaMemcpyHostToDevice, e->stream));
+  CK(e, cudaStreamSynchronize(e->stream));
+  return MCX_OK;
+}
+
+extern "C" mcx_status mcx_get_mask(mcx_engine *e, int r, int *pt, float *ns) {
+  if (mcx_status st = check_rep(e, r)) return st;
+  const RepDev &R = e->rep[r];
+  float *dns = e->d_stage;
+  launch_split_to_mask(R, e->d_pt, e->d_ns, e->d_stage_pt, dns, e->stream);
+  CKL(e);
+  if (pt) CK(e, cudaMemcpyAsync(pt, e->d_stage_pt, sizeof(int) * R.ntot, cudaMemcpyDeviceToHost, e->stream));
+  if (ns) CK(e, cudaMemcpyAsync(ns, dns, sizeof(float) * 3 * R.ntot, cudaMemcpyDeviceToHost, e->stream));
+  CK(e, cudaStreamSynchronize(e->stream));
+  return MCX_OK;
+}
+
+template <typename T>
+static mcx_status set_scalar(mcx_engine *e, int r, size_t off, T v, bool in_rep) {
+  if (!e) return fail(nullptr, MCX_ERR_INVALID, "null engine");
+  const int r0 = r < 0 ? 0 : r, r1 = r < 0 ? e->nrep : r + 1;
+  if (r >= e->nrep) return fail(e, MCX_ERR_INVALID, "replica %d out of range", r);
+  for (int q = r0; q < r1; q++) {
+    char *base = in_rep ? (char *)(e->d_rep + q) : (char *)(e->d_st + q);
+    CK(e, cudaMemcpyAsync(base + off, &v, sizeof(T), cudaMemcpyHostToDevice, e->stream));
+  }
+  CK(e, cudaStreamSynchronize(e->stream));
+  return MCX_OK;
+}
+
+extern "C" mcx_status mcx_set_temperature(mcx_engine *e, int r, float T) {
+  mcx_status st = set_scalar(e, r, offsetof(RepState, T), T, false);
+  if (!st && e)
+    for (int q = (r < 0 ? 0 : r); q < (r < 0 ? e->nrep : r + 1); q++) e->desc[q].T = T;
+  return st;
+}
+
+extern "C" mcx_status mcx_set_field(mcx_engine *e, int r, float E) {
+  if (e && !e->var.field) {
+    bool any = false;
+    for (int q = 0; q < e->nrep; q++) any |= e->desc[q].elecA != 0.f;
+    if (!any) return fail(e, MCX_ERR_UNSUPPORTED, "engine has no field term (elecA = 0 on every replica)");
+  }
+  mcx_status st = set_scalar(e, r, offsetof(RepDev, elecE), E, true);
+  if (!st && e)
+    for (int q = (r < 0 ? 0 : r); q < (r < 0 ? e->nrep : r + 1); q++) {
+      e->desc[q].elecE = E;
+      e->rep[q].elecE = E;
+    }
+  return st;
+}
+
+extern "C" mcx_status mcx_set_step(mcx_engine *e, int r, float a) {
+  return set_scalar(e, r, offsetof(RepState, ang_var), a, false);
+}
+
+// One sweep's kernels on e->stream.
+static void enqueue_sweep(mcx_engine *e, bool measure) {
+  PassArgs pa{};
+  pa.reps = e->d_rep;
+  pa.map = e->d_map;
+  pa.dir = e->d_dir;
+  pa.pt = e->d_pt;
+  pa.ns = e->d_ns;
+  pa.st = e->d_st;
+  const int nb = (int)e->map.size();
+  for (int c = 0; c < 2; c++) {
+    pa.colour = c;
+    launch_pass(e->var, pa, nb, false, e->stream);
+  }
+  EpilogueArgs ea{e->d_rep, e->d_st, e->d_macc, e->d_stats, e->d_series, e->series_cap, e->nrep};
+  if (measure) {
+    MeasureArgs ma{e->d_rep, e->d_map, e->d_dir, e->d_pt, e->d_ns, e->d_macc};
+    launch_measure(e->var, ma, nb, e->stream);
+  }
+  launch_epilogue(ea, measure, e->stream);
+}
+
+static mcx_status build_graph(mcx_engine *e, int measure) {
+  cudaGraph_t g;
+  CK(e, cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
+  for (int s = 0; s < kChunk; s++) enqueue_sweep(e, measure != 0);
+  cudaError_t lr = cudaGetLastError();
+  cudaError_t r = cudaStreamEndCapture(e->stream, &g);
+  if (lr != cudaSuccess) return fail(e, MCX_ERR_CUDA, "capture: %s", cudaGetErrorString(lr));
+  if (r != cudaSuccess) return fail(e, MCX_ERR_CUDA, "cudaStreamEndCapture: %s", cudaGetErrorString(r));
+  r = cudaGraphInstantiate(&e->graph[measure], g, 0);
+  cudaGraphDestroy(g);
+  if (r != cudaSuccess) return fail(e, MCX_ERR_CUDA, "cudaGraphInstantiate: %s", cudaGetErrorString(r));
+  e->graph_nodes[measure] = kChunk * (measure ? 4 : 3);
+  return MCX_OK;
+}
+
+extern "C" mcx_status mcx_sweep(mcx_engine *e, int n, int measure) {
+  if (!e) return fail(nullptr, MCX_ERR_INVALID, "null engine");
+  if (n < 0) return fail(e, MCX_ERR_INVALID, "negative sweep count");
+  const int m = measure ? 1 : 0;
+  if (n >= kChunk && !e->graph[m]) {
+    if (mcx_status st = build_graph(e, m)) return st;
+  }
+  int done = 0;
+  while (n - done >= kChunk) {
+    CK(e, cudaGraphLaunch(e->graph[m], e->stream));
+    e->launches += e->graph_nodes[m];
+    done += kChunk;
+  }
+  for (; done < n; done++) {
+    enqueue_sweep(e, m != 0);
+    e->launches += m ? 4 : 3;
+  }
+  CKL(e);
+  return MCX_OK;
+}
+
+extern "C" mcx_status mcx_sync(mcx_engine *e) {
+  if (!e) return fail(nullptr, MCX_ERR_INVALID, "null engine");
+  CK(e, cudaStreamSynchronize(e->stream));
+  return MCX_OK;
+}
+
+extern "C" mcx_status mcx_measure(mcx_engine *e, int r, double *out) {
+  if (mcx_status st = check_rep(e, r)) return st;
+  if (!out) return fail(e, MCX_ERR_INVALID, "null output");
+  MeasureArgs ma{e->d_rep, e->d_map, e->d_dir, e->d_pt, e->d_ns, e->d_macc};
+  launch_measure(e->var, ma, (int)e->map.size(), e->stream);
+  EpilogueArgs ea{e->d_rep, e->d_st, e->d_macc, e->d_stats, e->d_series, e->series_cap, e->nrep};
+  launch_measure_out(ea, e->d_mout, e->stream);
+  e->launches += 2;
+  CKL(e);
+  CK(e, cudaMemcpyAsync(out, e->d_mout + (size_t)r * 16, sizeof(double) * 16, cudaMemcpyDeviceToHost, e->stream));
+  CK(e, cudaStreamSynchronize(e->stream));
+  return MCX_OK;
+}
+
+extern "C" mcx_status mcx_get_stats(mcx_engine *e, int r, double *out) {
+  if (mcx_status st = check_rep(e, r)) return st;
+  if (!out) return fail(e, MCX_ERR_INVALID, "null output");
+  CK(e, cudaMemcpyAsync(out, e->d_stats + (size_t)r * kStats, sizeof(double) * kStats, cudaMemcpyDeviceToHost,
+                        e->stream));
+  CK(e, cudaStreamSynchronize(e->stream));
+  return MCX_OK;
+}
+
+extern "C" mcx_status mcx_reset_stats(mcx_engine *e, int r) {
+  if (!e) return fail(nullptr, MCX_ERR_INVALID, "null engine");
+  const int r0 = r < 0 ? 0 : r, r1 = r < 0 ? e->nrep : r + 1;
+  if (r >= e->nrep) return fail(e, MCX_ERR_INVALID, "replica %d out of range", r);
+  // keep the step size and sweep index entries (11, 12), clear the sums
+  for (int q = r0; q < r1; q++)
+    CK(e, cudaMemsetAsync(e->d_stats + (size_t)q * kStats, 0, sizeof(double) * 11, e->stream));
+  CK(e, cudaStreamSynchronize(e->stream));
+  return MCX_OK;
+}
+
+extern "C" mcx_status mcx_set_series(mcx_engine *e, int cap) {
+  if (!e) return fail(nullptr, MCX_ERR_INVALID, "null engine");
+  if (cap < 0) return fail(e, MCX_ERR_INVALID, "negative series capacity");
+  CK(e, cudaStreamSynchronize(e->stream));
+  cudaFree(e->d_series);
+  e->d_series = nullptr;
+  e->series_cap = 0;
+  if (cap > 0) {
+    cudaError_t r = cudaMalloc(&e->d_series, sizeof(double) * 2 * (size_t)cap * e->nrep);
+    if (r != cudaSuccess) return fail(e, MCX_ERR_NOMEM, "series buffer: %s", cudaGetErrorString(r));
+    CK(e, cudaMemset(e->d_series, 0, sizeof(double) * 2 * (size_t)cap * e->nrep));
+    e->series_cap = cap;
+  }
+  // the captured graphs hold the old series pointer
+  for (int m = 0; m < 2; m++)
+    if (e->graph[m]) {
+      cudaGraphExecDestroy(e->graph[m]);
+      e->graph[m] = nullptr;
+    }
+  return MCX_OK;
+}
+
+extern "C" mcx_status mcx_get_series(mcx_engine *e, int r, int count, double *out) {
+  if (mcx_status st = check_rep(e, r)) return st;
+  if (!out || count < 0) return fail(e, MCX_ERR_INVALID, "bad series request");
+  if (count > e->series_cap) return fail(e, MCX_ERR_INVALID, "count %d exceeds series capacity %d", count, e->series_cap);
+  double st[kStats];
+  if (mcx_status s = mcx_get_stats(e, r, st)) return s;
+  const long long n = (long long)st[0];
+  if (count > n) return fail(e, MCX_ERR_INVALID, "only %lld measured sweeps recorded", n);
+  std::vector<double> ring(2 * (size_t)e->series_cap);
+  CK(e, cudaMemcpy(ring.data(), e->d_series + (size_t)r * e->series_cap * 2, sizeof(double) * ring.size(),
+                   cudaMemcpyDeviceToHost));
+  for (int q = 0; q < count; q++) {
+    const long long idx = (n - count + q) % e->series_cap;
+    out[2 * q] = ring[2 * idx];
+    out[2 * q + 1] = ring[2 * idx + 1];
+  }
+  return MCX_OK;
+}
+
+extern "C" void *mcx_stream(mcx_engine *e) { return e ? (void *)e->stream : nullptr; }
+
+extern "C" mcx_status mcx_pass_timing(mcx_engine *e, int n, float *pass_ms, float *total_ms) {
+  if (!e) return fail(nullptr, MCX_ERR_INVALID, "null engine");
+  if (n <= 0) return fail(e, MCX_ERR_INVALID, "need n_sweeps > 0");
+  std::vector<cudaEvent_t> ev(4 * (size_t)n);
+  for (auto &x : ev) CK(e, cudaEventCreate(&x));
+  PassArgs pa{};
+  pa.reps = e->d_rep;
+  pa.map = e->d_map;
+  pa.dir = e->d_dir;
+  pa.pt = e->d_pt;
+  pa.ns = e->d_ns;
+  pa.st = e->d_st;
+  const int nb = (int)e->map.size();
+  EpilogueArgs ea{e->d_rep, e->d_st, e->d_macc, e->d_stats, e->d_series, e->series_cap, e->nrep};
+  for (int s = 0; s < n; s++) {
+    for (int c = 0; c < 2; c++) {
+      pa.colour = c;
+      CK(e, cudaEventRecord(ev[4 * s + 2 * c], e->stream));
+      launch_pass(e->var, pa, nb, false, e->stream);
+      CK(e, cudaEventRecord(ev[4 * s + 2 * c + 1], e->stream));
+    }
+    launch_epilogue(ea, false, e->stream);
+  }
+  e->launches += 3LL * n;
+  CKL(e);
+  CK(e, cudaStreamSynchronize(e->stream));
+  float sum = 0.f, t;
+  for (int q = 0; q < 2 * n; q++) {
+    CK(e, cudaEventElapsedTime(&t, ev[2 * q], ev[2 * q + 1]));
+    sum += t;
+  }
+  CK(e, cudaEventElapsedTime(&t, ev[0], ev.back()));
+  if (pass_ms) *pass_ms = sum;
+  if (total_ms) *total_ms = t;
+  for (auto &x : ev) cudaEventDestroy(x);
+  return MCX_OK;
+}
+
+extern "C" void mcx_ghrl_constants(float k11, float k22, float k33, float p0, float *out) {
+  ghrl_constants(k11, k22, k33, p0, out);
+}
+
+extern "C" mcx_status mcx_build_mask(const mcx_replica_desc *d, int *pt, float *ns) {
+  if (!d || !pt || !ns) return fail(nullptr, MCX_ERR_INVALID, "mcx_build_mask: null argument");
+  if (d->geometry == MCX_GEO_CUSTOM) return fail(nullptr, MCX_ERR_INVALID, "custom geometry comes from a file");
+  if (mcx_status st = check_desc(*d, 0)) return st;
+  std::vector<int> p;
+  std::vector<float> n;
+  build_mask(*d, p, n);
+  memcpy(pt, p.data(), sizeof(int) * p.size());
+  memcpy(ns, n.data(), sizeof(float) * n.size());
+  return MCX_OK;
+}
+
+extern "C" mcx_status mcx_read_geometry(const char *path, int nx, int ny, int nz, int *pt, float *ns, int *nsurf) {
+  if (!path || !pt || !ns || nx <= 0 || ny <= 0 || nz <= 0) return fail(nullptr, MCX_ERR_INVALID, "mcx_read_geometry: bad argument");
+  std::vector<int> p;
+  std::vector<float> n;
+  std::string err;
+  int k = read_custom_geometry(path, nx, ny, nz, p, n, err);
+  if (k < 0) return fail(nullptr, MCX_ERR_PARSE, "%s", err.c_str());
+  memcpy(pt, p.data(), sizeof(int) * p.size());
+  memcpy(ns, n.data(), sizeof(float) * n.size());
+  if (nsurf) *nsurf = k;
+  return MCX_OK;
+}
+
+extern "C" mcx_status mcx_debug_pass(mcx_engine *e, int r, int colour, float *dE, unsigned char *acc, float *prop) {
+  if (mcx_status st = check_rep(e, r)) return st;
+  if (colour != 0 && colour != 1) return fail(e, MCX_ERR_INVALID, "colour must be 0 or 1");
+  const RepDev &R = e->rep[r];
+  float *d_dE = nullptr, *d_prop = nullptr;
+  uint8_t *d_acc = nullptr;
+  int2 *d_map = nullptr;
+  std::vector<int2> sub;
+  for (const int2 &m : e->map)
+    if (m.x == r) sub.push_back(m);
+  CK(e, cudaMalloc(&d_dE, sizeof(float) * R.ntot));
+  CK(e, cudaMalloc(&d_prop, sizeof(float) * 3 * R.ntot));
+  CK(e, cudaMalloc(&d_acc, R.ntot));
+  CK(e, cudaMalloc(&d_map, sizeof(int2) * sub.size()));
+  CK(e, cudaMemsetAsync(d_dE, 0, sizeof(float) * R.ntot, e->stream));
+  CK(e, cudaMemsetAsync(d_prop, 0, sizeof(float) * 3 * R.ntot, e->stream));
+  CK(e, cudaMemsetAsync(d_acc, 0xFF, R.ntot, e->stream));
+  CK(e, cudaMemcpyAsync(d_map, sub.data(), sizeof(int2) * sub.size(), cudaMemcpyHostToDevice, e->stream));
+  PassArgs pa{};
+  pa.reps = e->d_rep;
+  pa.map = d_map;
+  pa.dir = e->d_dir;
+  pa.pt = e->d_pt;
+  pa.ns = e->d_ns;
+  pa.st = e->d_st;
+  pa.colour = colour;
+  pa.tr_dE = d_dE;
+  pa.tr_acc = d_acc;
+  pa.tr_prop = d_prop;
+  launch_pass(e->var, pa, (int)sub.size(), true, e->stream);
+  e->launches += 1;
+  CKL(e);
+  // a trace pass does not count toward the step-size rule
+  CK(e, cudaMemsetAsync(&e->d_st[r].acc, 0, sizeof(unsigned), e->stream));
+  if (dE) CK(e, cudaMemcpyAsync(dE, d_dE, sizeof(float) * R.ntot, cudaMemcpyDeviceToHost, e->stream));
+  if (acc) CK(e, cudaMemcpyAsync(acc, d_acc, R.ntot, cudaMemcpyDeviceToHost, e->stream));
+  if (prop) CK(e, cudaMemcpyAsync(prop, d_prop, sizeof(float) * 3 * R.ntot, cudaMemcpyDeviceToHost, e->stream));
+  CK(e, cudaStreamSynchronize(e->stream));
+  cudaFree(d_dE);
+  cudaFree(d_prop);
+  cudaFree(d_acc);
+  cudaFree(d_map);
+  return MCX_OK;
+}

@@ -1,0 +1,474 @@
+// mcx_sim.cpp -- the simulator driver behind mcx_run_file(): what
+// ./mc_sim <paramfile> does in the reference (src/main.cpp:63-83,
+// src/simulatorGPU.cpp:24-108, the run loops of src/evolve_{thermal,step,
+// quench,electric}.cu), over the GB300 engine.  The loops, their float
+// temperature stepping and the po.dat / director_field_*.csv formats follow
+// the reference; sweeps, E, Q and S run on the GPU.
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <strings.h>
+
+#include <algorithm>
+#include <string>
+#include <vector>
+
+#include "../../include/mcx.h"
+#include "mcx_host.h"
+
+namespace mcx {
+namespace {
+
+std::string g_err;
+
+struct Fail {
+  mcx_status st;
+};
+
+int anch_code(const std::string &s) {
+  static const char *names[] = {"homeotropic", "fg",      "rp",      "strong",
+                                "homeotropic_ghrl", "fg_ghrl", "rp_ghrl", "strong_ghrl"};
+  for (int i = 0; i < 8; i++)
+    if (strcasecmp(s.c_str(), names[i]) == 0) return i;
+  return -1;
+}
+
+bool ends_with_ci(const std::string &s, const char *suf, std::string &stem) {
+  size_t n = strlen(suf);
+  if (s.size() >= n && strcasecmp(s.c_str() + s.size() - n, suf) == 0) {
+    stem = s.substr(0, s.size() - n);
+    return true;
+  }
+  return false;
+}
+
+// Local order parameter of one site (lattice_order_parameter,
+// src/parameter_order.cpp:62-113): Q over the site and its existing active
+// neighbours, largest eigenvalue by cyclic Jacobi.
+double local_S(const std::vector<float> &ni, const std::vector<int> &pt, int nx, int ny, int nz, int xb, int yb, int zb,
+               int i, int j, int k) {
+  double Q[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  int points = 0;
+  const int d[7][3] = {{0, 0, 0}, {-1, 0, 0}, {1, 0, 0}, {0, -1, 0}, {0, 1, 0}, {0, 0, -1}, {0, 0, 1}};
+  for (int q = 0; q < 7; q++) {
+    int ii = i + d[q][0], jj = j + d[q][1], kk = k + d[q][2];
+    auto wrap = [](int &x, int n, int b) {
+      if (x < 0 || x >= n) {
+        if (b == MCX_BOUND_PERIODIC) x = (x + n) % n;
+        else return false;
+      }
+      return true;
+    };
+    if (!wrap(ii, nx, xb) || !wrap(jj, ny, yb) || !wrap(kk, nz, zb)) continue;
+    const long s = (long)ii + (long)nx * ((long)jj + (long)ny * kk);
+    if (pt[s] == 0) continue;
+    const double n[3] = {ni[3 * s], ni[3 * s + 1], ni[3 * s + 2]};
+    for (int l = 0; l < 3; l++) {
+      for (int m = 0; m <= l; m++) Q[3 * m + l] += 3.0 * n[l] * n[m];
+      Q[4 * l] -= 1;
+    }
+    points++;
+  }
+  for (int c : {0, 1, 2, 4, 5, 8}) Q[c] /= 2.0 * points;
+  Q[3] = Q[1];
+  Q[6] = Q[2];
+  Q[7] = Q[5];
+  double A[3][3];
+  for (int r = 0; r < 3; r++)
+    for (int c = 0; c < 3; c++) A[r][c] = Q[3 * r + c];
+  for (int it = 0; it < 50; it++) {
+    double off = fabs(A[0][1]) + fabs(A[0][2]) + fabs(A[1][2]);
+    if (off < 1e-15) break;
+    for (int p = 0; p < 2; p++)
+      for (int qq = p + 1; qq < 3; qq++) {
+        if (A[p][qq] == 0) continue;
+        double th = (A[qq][qq] - A[p][p]) / (2 * A[p][qq]);
+        double t = (th >= 0 ? 1 : -1) / (fabs(th) + sqrt(th * th + 1));
+        double c = 1 / sqrt(t * t + 1), s = t * c;
+        for (int r = 0; r < 3; r++) { double x = A[r][p], y = A[r][qq]; A[r][p] = c * x - s * y; A[r][qq] = s * x + c * y; }
+        for (int r = 0; r < 3; r++) { double x = A[p][r], y = A[qq][r]; A[p][r] = c * x - s * y; A[qq][r] = s * x + c * y; }
+      }
+  }
+  return fmax(A[0][0], fmax(A[1][1], A[2][2]));
+}
+
+// print_n (src/io.cpp:50-80): x,y,z,nx,ny,nz,S,pt with S = nan on inactive sites.
+bool write_snapshot(const std::string &path, const std::vector<float> &ni, const std::vector<int> &pt,
+                    const mcx_replica_desc &d, bool with_S) {
+  FILE *f = fopen(path.c_str(), "w");
+  if (!f) return false;
+  fprintf(f, with_S ? "x,y,z,nx,ny,nz,S,pt\n" : "x,y,z,nx,ny,nz,s,pt\n");
+  for (int k = 0; k < d.nz; k++)
+    for (int j = 0; j < d.ny; j++)
+      for (int i = 0; i < d.nx; i++) {
+        const long s = (long)i + (long)d.nx * ((long)j + (long)d.ny * k);
+        if (with_S) {
+          const double S = pt[s] ? local_S(ni, pt, d.nx, d.ny, d.nz, d.xbound, d.ybound, d.zbound, i, j, k) : NAN;
+          fprintf(f, "%d,%d,%d,%g,%g,%g,%g,%d\n", i, j, k, ni[3 * s], ni[3 * s + 1], ni[3 * s + 2], (float)S, pt[s]);
+        } else {
+          fprintf(f, "%d,%d,%d,%g,%g,%g,1,%d\n", i, j, k, ni[3 * s], ni[3 * s + 1], ni[3 * s + 2], pt[s]);
+        }
+      }
+  fclose(f);
+  return true;
+}
+
+// read_ic_file (src/ic.cpp:88-119): header line, then x,y,z,nx,ny,nz rows.
+bool read_ic_file(const std::string &path, const mcx_replica_desc &d, std::vector<float> &ni, std::string &err) {
+  FILE *f = fopen(path.c_str(), "r");
+  if (!f) {
+    err = "cannot open ic_file " + path;
+    return false;
+  }
+  char buf[512];
+  if (!fgets(buf, sizeof buf, f)) {
+    fclose(f);
+    err = "empty ic_file";
+    return false;
+  }
+  const long n = (long)d.nx * d.ny * d.nz;
+  for (long q = 0; q < n; q++) {
+    int x, y, z;
+    float a, b, c;
+    if (!fgets(buf, sizeof buf, f) || sscanf(buf, "%d,%d,%d,%f,%f,%f", &x, &y, &z, &a, &b, &c) != 6) {
+      fclose(f);
+      err = "malformed ic_file line " + std::to_string(q + 2);
+      return false;
+    }
+    if (x < 0 || y < 0 || z < 0 || x >= d.nx || y >= d.ny || z >= d.nz) {
+      fclose(f);
+      err = "ic_file point out of the box at line " + std::to_string(q + 2);
+      return false;
+    }
+    const long s = (long)x + (long)d.nx * ((long)y + (long)d.ny * z);
+    ni[3 * s] = a;
+    ni[3 * s + 1] = b;
+    ni[3 * s + 2] = c;
+  }
+  fclose(f);
+  return true;
+}
+
+// Reads and validates a parameter file into replica 0's descriptor, the
+// custom mask (if any) and the mode index (0 thermal, 1 step, 2 quench,
+// 3 electric).
+mcx_status prepare(const char *path, SimParams &P, mcx_replica_desc &d, std::vector<int> &cpt, std::vector<float> &cns,
+                   int &im) {
+  std::string err;
+  int rc = parse_param_file(path, P, err);
+  if (rc) {
+    g_err = err;
+    return (mcx_status)rc;
+  }
+  memset(&d, 0, sizeof d);
+  d.nx = P.Nx;
+  d.ny = P.Ny;
+  d.nz = P.Nz;
+  if (strcasecmp(P.geometry.c_str(), "bulk") == 0) d.geometry = MCX_GEO_BULK;
+  else if (strcasecmp(P.geometry.c_str(), "slab") == 0) d.geometry = MCX_GEO_SLAB;
+  else if (strcasecmp(P.geometry.c_str(), "sphere") == 0) d.geometry = MCX_GEO_SPHERE;
+  else if (strcasecmp(P.geometry.c_str(), "custom") == 0) d.geometry = MCX_GEO_CUSTOM;
+  else {
+    g_err = "geometry '" + P.geometry + "' not implemented. Options: bulk | slab | sphere | custom";
+    return MCX_ERR_PARSE;
+  }
+  auto bound = [&](const std::string &s, int &out, const char *ax) {
+    if (strcasecmp(s.c_str(), "free") == 0) out = MCX_BOUND_FREE;
+    else if (strcasecmp(s.c_str(), "periodic") == 0) out = MCX_BOUND_PERIODIC;
+    else {
+      g_err = std::string(ax) + " boundary '" + s + "' not implemented. Options: free | periodic";
+      return false;
+    }
+    return true;
+  };
+  if (!bound(P.xbound, d.xbound, "X") || !bound(P.ybound, d.ybound, "Y") || !bound(P.zbound, d.zbound, "Z"))
+    return MCX_ERR_PARSE;
+  if (strcasecmp(P.potential.c_str(), "ll") == 0 || strcasecmp(P.potential.c_str(), "lebwohl-lahser") == 0)
+    d.potential = MCX_POT_LL;
+  else if (strcasecmp(P.potential.c_str(), "ghrl") == 0 || strcasecmp(P.potential.c_str(), "grun-hess") == 0)
+    d.potential = MCX_POT_GHRL;
+  else if (strcasecmp(P.potential.c_str(), "pear") == 0) {
+    g_err = "potential 'pear' is not implemented by the GB300 engine";
+    return MCX_ERR_UNSUPPORTED;
+  } else {
+    g_err = "potential '" + P.potential + "' not implemented. Options: ll | ghrl";
+    return MCX_ERR_PARSE;
+  }
+  d.A = P.A;
+  d.k11 = P.k11;
+  d.k22 = P.k22;
+  d.k33 = P.k33;
+  d.p0 = P.p0;
+  d.elecA = P.elecA;
+  d.elecX = P.elecX;
+  d.elecY = P.elecY;
+  d.elecZ = P.elecZ;
+  d.elecE = P.elecE;
+  d.T = P.Ti;
+  d.ang_var = 0.5f;  // src/evolve_thermal.cpp:36
+  d.radius = P.radius;
+  int nsurf = d.geometry == MCX_GEO_SLAB ? 2 : d.geometry == MCX_GEO_SPHERE ? 1 : 0;
+  if (d.geometry == MCX_GEO_CUSTOM) {
+    nsurf = read_custom_geometry(P.bound_file.c_str(), d.nx, d.ny, d.nz, cpt, cns, err);
+    if (nsurf < 0) {
+      g_err = err;
+      return MCX_ERR_PARSE;
+    }
+  }
+  if (nsurf > MCX_MAX_SURFACES) {
+    g_err = "more than 16 surfaces";
+    return MCX_ERR_UNSUPPORTED;
+  }
+  d.n_surfaces = nsurf;
+  for (int s = 0; s < nsurf; s++) {  // Geometry::Boundary_Init (src/geometry.cpp:73-103)
+    if (!P.anchoring_type.count(s)) {
+      g_err = "you must define " + std::to_string(nsurf) + " boundaries (anchoring_type " + std::to_string(s) + " missing)";
+      return MCX_ERR_PARSE;
+    }
+    const int a = anch_code(P.anchoring_type[s]);
+    if (a < 0) {
+      g_err = P.anchoring_type[s] + " boundary condition is not defined";
+      return MCX_ERR_PARSE;
+    }
+    d.anchoring[s] = a;
+    if (!P.W.count(s)) {
+      g_err = "parameter W not defined for boundary condition #" + std::to_string(s);
+      return MCX_ERR_PARSE;
+    }
+    d.W[s] = P.W[s];
+    const bool needs_axis = a == MCX_ANCH_RP || a == MCX_ANCH_STRONG || a == MCX_ANCH_RP_GHRL || a == MCX_ANCH_STRONG_GHRL;
+    if (needs_axis && (!P.phi_s.count(s) || !P.theta_s.count(s))) {
+      g_err = "parameters phi_s/theta_s not defined for boundary condition #" + std::to_string(s);
+      return MCX_ERR_PARSE;
+    }
+    d.phi_s[s] = P.phi_s.count(s) ? P.phi_s[s] : 0.f;
+    d.theta_s[s] = P.theta_s.count(s) ? P.theta_s[s] : 0.f;
+  }
+  std::string stem, mode = P.evol;
+  if (ends_with_ci(mode, "GPU", stem) || ends_with_ci(mode, "GB300", stem)) mode = stem;
+  const char *modes[] = {"thermal", "step", "quench", "electric"};
+  im = -1;
+  for (int q = 0; q < 4; q++)
+    if (strcasecmp(mode.c_str(), modes[q]) == 0) im = q;
+  if (im < 0) {
+    g_err = "evol mode '" + P.evol + "' not implemented. Options: thermal | step | quench | electric (GPU / GB300 suffix accepted)";
+    return MCX_ERR_PARSE;
+  }
+  if (d.nx % 2) {
+    g_err = "Nx = " + std::to_string(d.nx) + " must be even for red/black sweeps";
+    return MCX_ERR_UNSUPPORTED;
+  }
+  if (im == 0 && P.dT == 0) {
+    g_err = "dT must be non-zero";
+    return MCX_ERR_PARSE;
+  }
+  if (im == 3 && P.elecdE == 0) {
+    g_err = "dE must be non-zero";
+    return MCX_ERR_PARSE;
+  }
+  if (P.replicas < 1) {
+    g_err = "replicas must be >= 1";
+    return MCX_ERR_PARSE;
+  }
+  return MCX_OK;
+}
+
+mcx_status run(const char *path, const char *out_dir) {
+  SimParams P;
+  mcx_replica_desc d;
+  std::vector<int> cpt;
+  std::vector<float> cns;
+  int im;
+  std::string err;
+  if (mcx_status st = prepare(path, P, d, cpt, cns, im)) return st;
+  const std::string dir = out_dir ? std::string(out_dir) + "/" : std::string();
+  const int R = P.replicas > 0 ? P.replicas : 1;
+  std::vector<mcx_replica_desc> descs(R, d);
+  for (int r = 0; r < R; r++) {
+    descs[r].seed = (unsigned)(P.seed + r);
+    descs[r].stream = (unsigned)r;
+  }
+  mcx_engine *e = nullptr;
+  mcx_status st = mcx_create(R, descs.data(), &e);
+  if (st) {
+    g_err = mcx_last_error(nullptr);
+    return st;
+  }
+  struct Guard {
+    mcx_engine *e;
+    ~Guard() { mcx_destroy(e); }
+  } guard{e};
+  auto check = [&](mcx_status s) {
+    if (s) {
+      g_err = mcx_last_error(e);
+      throw Fail{s};
+    }
+  };
+  const long nsites = (long)d.nx * d.ny * d.nz;
+  std::vector<float> ni(3 * nsites);
+  std::vector<int> pt(nsites);
+  std::vector<float> ns(3 * nsites);
+  try {
+    for (int r = 0; r < R; r++) {
+      if (d.geometry == MCX_GEO_CUSTOM) check(mcx_set_mask(e, r, cpt.data(), cns.data()));
+      if (strcasecmp(P.ic.c_str(), "random") == 0) {
+        check(mcx_init_random(e, r, descs[r].seed));
+      } else if (strcasecmp(P.ic.c_str(), "homogeneous") == 0) {
+        check(mcx_init_homogeneous(e, r, P.theta_0, P.phi_0));
+      } else if (strcasecmp(P.ic.c_str(), "ic_file") == 0) {
+        std::fill(ni.begin(), ni.end(), 0.f);
+        if (!read_ic_file(P.ic_file, d, ni, err)) {
+          g_err = err;
+          return MCX_ERR_PARSE;
+        }
+        check(mcx_set_state(e, r, ni.data()));
+      } else if (strcasecmp(P.ic.c_str(), "cholesteric") == 0) {  // src/ic.cpp:121-151
+        check(mcx_get_mask(e, r, pt.data(), ns.data()));
+        const float theta = P.theta_0;
+        const float phi0 = (float)(P.phi_0 * M_PI / 180);
+        const float p0 = P.p0_i != 0 ? P.p0_i : P.p0;
+        for (int k = 0; k < d.nz; k++)
+          for (int j = 0; j < d.ny; j++)
+            for (int i = 0; i < d.nx; i++) {
+              const long s = (long)i + (long)d.nx * ((long)j + (long)d.ny * k);
+              if (pt[s]) {
+                const float phi = (float)(phi0 - 2 * M_PI * k / p0);
+                ni[3 * s] = (float)(sin(theta * M_PI / 180) * cos(phi));
+                ni[3 * s + 1] = (float)(sin(theta * M_PI / 180) * sin(phi));
+                ni[3 * s + 2] = (float)cos(theta * M_PI / 180);
+              } else {
+                ni[3 * s] = 0;
+                ni[3 * s + 1] = 0;
+                ni[3 * s + 2] = 1;
+              }
+            }
+        check(mcx_set_state(e, r, ni.data()));
+      } else {
+        g_err = "initial condition '" + P.ic + "' not implemented. Options: random | homogeneous | ic_file | cholesteric";
+        return MCX_ERR_PARSE;
+      }
+    }
+    check(mcx_get_mask(e, 0, pt.data(), ns.data()));
+    check(mcx_get_state(e, 0, ni.data()));
+    write_snapshot(dir + "ic.csv", ni, pt, descs[0], false);
+    std::vector<FILE *> po(R, nullptr);
+    for (int r = 0; r < R; r++) {
+      std::string name = r == 0 ? dir + "po.dat" : dir + "po_r" + std::to_string(r) + ".dat";
+      po[r] = fopen(name.c_str(), "a");
+      if (!po[r]) {
+        g_err = "cannot open " + name;
+        for (FILE *f : po)
+          if (f) fclose(f);
+        return MCX_ERR_IO;
+      }
+      fprintf(po[r], im == 0 || im == 3 ? "T S varS E varE\n" : "ii S varS E varE\n");
+      fflush(po[r]);
+    }
+    struct PoGuard {
+      std::vector<FILE *> &v;
+      ~PoGuard() {
+        for (FILE *f : v)
+          if (f) fclose(f);
+      }
+    } pog{po};
+    double stt[MCX_STATS_LEN];
+    // one block: MCT thermalisation sweeps, MCS measured sweeps, a po.dat row
+    auto block = [&](int n_therm, const char *label_fmt, double label, int ilabel, const std::string &snap) {
+      check(mcx_sweep(e, n_therm, 0));
+      check(mcx_reset_stats(e, -1));
+      check(mcx_sweep(e, P.MCS, 1));
+      for (int r = 0; r < R; r++) {
+        check(mcx_get_stats(e, r, stt));
+        const double n = stt[MCX_ST_N] > 0 ? stt[MCX_ST_N] : 1;
+        const double S1 = stt[MCX_ST_S1] / n, S2 = stt[MCX_ST_S2] / n;
+        const double E = stt[MCX_ST_E1] / n, E2 = stt[MCX_ST_E2] / n;
+        if (label_fmt[1] == 'd')
+          fprintf(po[r], "%d %g %g %g %g\n", ilabel, S1, S2 - S1 * S1, E, E2 - E * E);
+        else
+          fprintf(po[r], "%g %g %g %g %g\n", label, S1, S2 - S1 * S1, E, E2 - E * E);
+        fflush(po[r]);
+      }
+      if (!snap.empty()) {
+        check(mcx_get_state(e, 0, ni.data()));
+        write_snapshot(snap, ni, pt, descs[0], true);
+      }
+    };
+    const bool snapshots = getenv("MCX_NO_SNAPSHOTS") == nullptr;
+    if (im == 0) {  // thermal (src/evolve_thermal.cu:79-110)
+      if (P.dT == 0) {
+        g_err = "dT must be non-zero";
+        return MCX_ERR_PARSE;
+      }
+      const int sign = (int)(-P.dT / fabsf(P.dT));
+      for (float T = P.Ti; (int)1e6 * sign * (T - P.Tf) >= 0; T += P.dT) {
+        check(mcx_set_temperature(e, -1, T));
+        std::string snap = snapshots ? dir + "director_field_" + std::to_string((int)(100 * (T + 1e-7))) + ".csv" : "";
+        block(P.MCT, "%g", T, 0, snap);
+      }
+    } else if (im == 3) {  // electric (src/evolve_electric.cpp:59-90)
+      if (P.elecdE == 0) {
+        g_err = "dE must be non-zero";
+        return MCX_ERR_PARSE;
+      }
+      check(mcx_set_temperature(e, -1, P.Ti));
+      const int sign = (int)(-P.elecdE / fabsf(P.elecdE));
+      for (float E = P.elecEi; (int)1e6 * sign * (E - P.elecEf) >= 0; E += P.elecdE) {
+        check(mcx_set_field(e, -1, E));
+        std::string snap = snapshots ? dir + "director_field_" + std::to_string((int)(100 * (E + 1e-7))) + ".csv" : "";
+        block(P.MCT, "%g", E, 0, snap);
+      }
+    } else {  // step / quench (src/evolve_step.cpp:58-90, src/evolve_quench.cpp:58-94)
+      check(mcx_set_temperature(e, -1, P.Ti));
+      for (int ii = P.first_file; ii < P.fn + P.first_file; ii++) {
+        int n_therm = P.MCT;
+        if (im == 2) {
+          check(mcx_set_temperature(e, -1, P.Ti));
+          check(mcx_sweep(e, P.MCT, 0));
+          check(mcx_set_temperature(e, -1, P.Tf));
+          n_therm = 0;
+          for (int step = 0; step < P.MCT * P.dT; step++) n_therm++;  // MCT*dT sweeps (float bound)
+        }
+        std::string snap = snapshots ? dir + "director_field_" + std::to_string(ii) + ".csv" : "";
+        block(n_therm, "%d", 0, ii, snap);
+      }
+    }
+  } catch (const Fail &f) {
+    return f.st;
+  }
+  return MCX_OK;
+}
+
+}  // namespace
+}  // namespace mcx
+
+extern "C" mcx_status mcx_run_file(const char *param_file, const char *out_dir) {
+  if (!param_file) {
+    mcx::set_last_error("mcx_run_file: null parameter file");
+    return MCX_ERR_INVALID;
+  }
+  mcx::g_err.clear();
+  mcx_status st = mcx::run(param_file, out_dir);
+  if (st) mcx::set_last_error(mcx::g_err.c_str());
+  return st;
+}
+
+extern "C" mcx_status mcx_check_file(const char *param_file, mcx_replica_desc *desc) {
+  if (!param_file) {
+    mcx::set_last_error("mcx_check_file: null parameter file");
+    return MCX_ERR_INVALID;
+  }
+  mcx::g_err.clear();
+  mcx::SimParams P;
+  mcx_replica_desc d;
+  std::vector<int> cpt;
+  std::vector<float> cns;
+  int im;
+  mcx_status st = mcx::prepare(param_file, P, d, cpt, cns, im);
+  if (st) {
+    mcx::set_last_error(mcx::g_err.c_str());
+    return st;
+  }
+  if (desc) *desc = d;
+  return MCX_OK;
+}

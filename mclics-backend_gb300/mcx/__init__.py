@@ -1,0 +1,278 @@
+"""Python host interface to the GB300 Metropolis engine for the McLiCS
+nematic lattice model: ctypes over the C ABI in include/mcx.h
+(_build/libmcx.so).
+
+The engine runs only on the GPU: importing works anywhere, but creating an
+Engine needs the compiled library and a CUDA device, and fails loudly
+otherwise -- there is no CPU fallback.
+
+Names follow the reference's parameter keys (include/parameters.h:11-83);
+directors cross the boundary in the reference's AoS layout
+ni[(i + Nx*(j + Ny*k)), 0:3] (include/define.h:10-12).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Dict, Iterable, List, Optional, Sequence
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.dirname(HERE)
+LIB_PATH = os.path.join(PKG, "_build", "libmcx.so")
+CLI_PATH = os.path.join(PKG, "_build", "mc_sim_gb300")
+
+MAX_SURFACES = 16
+POTENTIALS = {"ll": 0, "lebwohl-lahser": 0, "ghrl": 1, "grun-hess": 1}
+GEOMETRIES = {"bulk": 0, "slab": 1, "sphere": 2, "custom": 3}
+BOUNDS = {"free": 0, "periodic": 1}
+ANCHORINGS = {"homeotropic": 0, "fg": 1, "rp": 2, "strong": 3, "homeotropic_ghrl": 4, "fg_ghrl": 5, "rp_ghrl": 6,
+              "strong_ghrl": 7}
+STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "out of memory", 4: "unsupported", 5: "I/O error",
+          6: "parse error"}
+
+# mcx_measure / mcx_get_stats layouts
+M_E, M_E_VALID, M_Q, M_S, M_DIRECTOR, M_VALID = 0, 1, 2, 11, 12, 15
+ST_N, ST_S1, ST_S2, ST_E1, ST_E2, ST_EV1, ST_EV2, ST_ACC, ST_SWEEPS, ST_LAST_E, ST_LAST_S, ST_ANG_VAR, ST_SWEEP_INDEX = \
+    range(13)
+
+
+class McxError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"mcx: {STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+class ReplicaDesc(C.Structure):
+    _fields_ = [
+        ("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int),
+        ("geometry", C.c_int),
+        ("xbound", C.c_int), ("ybound", C.c_int), ("zbound", C.c_int),
+        ("potential", C.c_int),
+        ("A", C.c_float),
+        ("k11", C.c_float), ("k22", C.c_float), ("k33", C.c_float), ("p0", C.c_float),
+        ("elecA", C.c_float), ("elecX", C.c_float), ("elecY", C.c_float), ("elecZ", C.c_float), ("elecE", C.c_float),
+        ("T", C.c_float),
+        ("ang_var", C.c_float),
+        ("seed", C.c_uint), ("stream", C.c_uint),
+        ("n_surfaces", C.c_int),
+        ("anchoring", C.c_int * MAX_SURFACES),
+        ("W", C.c_float * MAX_SURFACES),
+        ("theta_s", C.c_float * MAX_SURFACES),
+        ("phi_s", C.c_float * MAX_SURFACES),
+        ("radius", C.c_float),
+    ]
+
+
+def replica(nx=16, ny=16, nz=16, geometry="bulk", xbound="periodic", ybound="periodic", zbound="periodic",
+            potential="ll", A=1.0, k11=1.0, k22=1.0, k33=1.0, p0=0.0, elecA=0.0, elecX=0.0, elecY=0.0, elecZ=0.0,
+            elecE=1.0, T=1.0, ang_var=0.5, seed=1, stream=0, surfaces: Sequence[dict] = (), radius=0.0) -> ReplicaDesc:
+    """A replica descriptor from the reference's parameter names.  `surfaces`
+    is a list of dicts with keys anchoring, W, theta_s, phi_s (surface id =
+    list index = pt - 2)."""
+    d = ReplicaDesc()
+    d.nx, d.ny, d.nz = nx, ny, nz
+    d.geometry = GEOMETRIES[geometry.lower()]
+    d.xbound, d.ybound, d.zbound = BOUNDS[xbound.lower()], BOUNDS[ybound.lower()], BOUNDS[zbound.lower()]
+    d.potential = POTENTIALS[potential.lower()]
+    d.A, d.k11, d.k22, d.k33, d.p0 = A, k11, k22, k33, p0
+    d.elecA, d.elecX, d.elecY, d.elecZ, d.elecE = elecA, elecX, elecY, elecZ, elecE
+    d.T, d.ang_var, d.seed, d.stream = T, ang_var, seed, stream
+    d.n_surfaces = len(surfaces)
+    for i, s in enumerate(surfaces):
+        d.anchoring[i] = ANCHORINGS[s.get("anchoring", "homeotropic").lower()]
+        d.W[i] = s.get("W", 1.0)
+        d.theta_s[i] = s.get("theta_s", 0.0)
+        d.phi_s[i] = s.get("phi_s", 0.0)
+    d.radius = radius
+    return d
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    """The engine library; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise McxError(5, f"{LIB_PATH} is missing: build it with mclics-backend_gb300/build.py")
+        L = C.CDLL(LIB_PATH)
+        V, I, F, D = C.c_void_p, C.c_int, C.c_float, C.c_double
+        L.mcx_version.restype = I
+        L.mcx_last_error.restype = C.c_char_p
+        L.mcx_last_error.argtypes = [V]
+        L.mcx_create.argtypes = [I, C.POINTER(ReplicaDesc), C.POINTER(V)]
+        L.mcx_destroy.argtypes = [V]
+        L.mcx_num_replicas.argtypes = [V]
+        L.mcx_get_desc.argtypes = [V, I, C.POINTER(ReplicaDesc), V]
+        for name in ("mcx_set_state", "mcx_get_state"):
+            getattr(L, name).argtypes = [V, I, V]
+        L.mcx_init_random.argtypes = [V, I, C.c_uint]
+        L.mcx_init_homogeneous.argtypes = [V, I, F, F]
+        L.mcx_set_mask.argtypes = [V, I, V, V]
+        L.mcx_get_mask.argtypes = [V, I, V, V]
+        L.mcx_set_temperature.argtypes = [V, I, F]
+        L.mcx_set_field.argtypes = [V, I, F]
+        L.mcx_set_step.argtypes = [V, I, F]
+        L.mcx_sweep.argtypes = [V, I, I]
+        L.mcx_sync.argtypes = [V]
+        L.mcx_measure.argtypes = [V, I, V]
+        L.mcx_get_stats.argtypes = [V, I, V]
+        L.mcx_reset_stats.argtypes = [V, I]
+        L.mcx_set_series.argtypes = [V, I]
+        L.mcx_get_series.argtypes = [V, I, I, V]
+        L.mcx_debug_pass.argtypes = [V, I, I, V, V, V]
+        L.mcx_kernel_launches.argtypes = [V]
+        L.mcx_kernel_launches.restype = C.c_longlong
+        L.mcx_run_file.argtypes = [C.c_char_p, C.c_char_p]
+        _lib = L
+    return _lib
+
+
+def _p(a: np.ndarray):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+class Engine:
+    """A batch of replicas resident on the GPU (mcx_create ... mcx_destroy)."""
+
+    def __init__(self, descs: Iterable[ReplicaDesc]):
+        descs = list(descs)
+        arr = (ReplicaDesc * len(descs))(*descs)
+        h = C.c_void_p()
+        self._L = lib()
+        st = self._L.mcx_create(len(descs), arr, C.byref(h))
+        if st:
+            raise McxError(st, self._L.mcx_last_error(None).decode())
+        self._h = h
+        self.descs = descs
+        self.n = len(descs)
+
+    def _ck(self, st: int):
+        if st:
+            raise McxError(st, self._L.mcx_last_error(self._h).decode())
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.mcx_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def sites(self, r: int) -> int:
+        d = self.descs[r]
+        return d.nx * d.ny * d.nz
+
+    def desc(self, r: int):
+        d = ReplicaDesc()
+        g = np.zeros(5, np.float32)
+        self._ck(self._L.mcx_get_desc(self._h, r, C.byref(d), _p(g)))
+        return d, g
+
+    def set_state(self, r: int, ni: np.ndarray):
+        ni = np.ascontiguousarray(ni, dtype=np.float32).reshape(-1, 3)
+        if ni.shape[0] != self.sites(r):
+            raise ValueError("director array has the wrong number of sites")
+        self._ck(self._L.mcx_set_state(self._h, r, _p(ni)))
+
+    def get_state(self, r: int) -> np.ndarray:
+        out = np.empty((self.sites(r), 3), np.float32)
+        self._ck(self._L.mcx_get_state(self._h, r, _p(out)))
+        return out
+
+    def init_random(self, r: int, seed: int):
+        self._ck(self._L.mcx_init_random(self._h, r, seed))
+
+    def init_homogeneous(self, r: int, theta_0: float = 0.0, phi_0: float = 0.0):
+        self._ck(self._L.mcx_init_homogeneous(self._h, r, theta_0, phi_0))
+
+    def set_mask(self, r: int, pt: np.ndarray, ns: Optional[np.ndarray] = None):
+        pt = np.ascontiguousarray(pt, dtype=np.int32).reshape(-1)
+        nsp = None
+        if ns is not None:
+            ns = np.ascontiguousarray(ns, dtype=np.float32).reshape(-1, 3)
+            nsp = _p(ns)
+        self._ck(self._L.mcx_set_mask(self._h, r, _p(pt), nsp))
+
+    def get_mask(self, r: int):
+        pt = np.empty(self.sites(r), np.int32)
+        ns = np.empty((self.sites(r), 3), np.float32)
+        self._ck(self._L.mcx_get_mask(self._h, r, _p(pt), _p(ns)))
+        return pt, ns
+
+    def set_temperature(self, T: float, r: int = -1):
+        self._ck(self._L.mcx_set_temperature(self._h, r, T))
+
+    def set_field(self, E: float, r: int = -1):
+        self._ck(self._L.mcx_set_field(self._h, r, E))
+
+    def set_step(self, ang_var: float, r: int = -1):
+        self._ck(self._L.mcx_set_step(self._h, r, ang_var))
+
+    def sweep(self, n: int, measure: bool = False):
+        self._ck(self._L.mcx_sweep(self._h, n, 1 if measure else 0))
+
+    def sync(self):
+        self._ck(self._L.mcx_sync(self._h))
+
+    def measure(self, r: int) -> Dict:
+        out = np.zeros(16)
+        self._ck(self._L.mcx_measure(self._h, r, _p(out)))
+        return dict(E=out[M_E], E_valid=out[M_E_VALID], Q=out[M_Q:M_Q + 9].reshape(3, 3), S=out[M_S],
+                    director=out[M_DIRECTOR:M_DIRECTOR + 3], valid=int(out[M_VALID]))
+
+    def stats(self, r: int) -> np.ndarray:
+        out = np.zeros(16)
+        self._ck(self._L.mcx_get_stats(self._h, r, _p(out)))
+        return out
+
+    def reset_stats(self, r: int = -1):
+        self._ck(self._L.mcx_reset_stats(self._h, r))
+
+    def set_series(self, capacity: int):
+        self._ck(self._L.mcx_set_series(self._h, capacity))
+
+    def series(self, r: int, count: int) -> np.ndarray:
+        out = np.zeros((count, 2))
+        self._ck(self._L.mcx_get_series(self._h, r, count, _p(out)))
+        return out
+
+    def debug_pass(self, r: int, colour: int):
+        n = self.sites(r)
+        dE = np.zeros(n, np.float32)
+        acc = np.zeros(n, np.uint8)
+        prop = np.zeros((n, 3), np.float32)
+        self._ck(self._L.mcx_debug_pass(self._h, r, colour, _p(dE), _p(acc), _p(prop)))
+        return dE, acc, prop
+
+    @property
+    def kernel_launches(self) -> int:
+        return int(self._L.mcx_kernel_launches(self._h))
+
+
+def run_file(param_file: str, out_dir: Optional[str] = None) -> None:
+    """./mc_sim <param_file> on the GPU (src/main.cpp:63-83 of the reference)."""
+    L = lib()
+    st = L.mcx_run_file(param_file.encode(), out_dir.encode() if out_dir else None)
+    if st:
+        raise McxError(st, L.mcx_last_error(None).decode())
+
+
+def exported_symbols() -> List[str]:
+    """Every entry point declared in include/mcx.h."""
+    hdr = os.path.join(os.path.dirname(PKG), "include", "mcx.h")
+    import re
+    names = re.findall(r"\b(mcx_[a-z_]+)\s*\(", open(hdr).read())
+    return sorted(set(names))

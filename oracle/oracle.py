@@ -183,6 +183,7 @@ def lib():
         L.orc_pass.argtypes = [P, V, V, V, F, F, C.c_uint32, C.c_uint32, C.c_uint64, I, I, I, D, V,
                                C.POINTER(_Trace)]
         L.orc_pass.restype = C.c_long
+        L.orc_propose.argtypes = [V, D, D, F, I, V]
         L.orc_adapt.argtypes = [F, C.c_long, C.c_long]
         L.orc_adapt.restype = F
         L.orc_sweep.argtypes = [P, V, V, V, F, C.POINTER(F), C.c_uint32, C.c_uint32, C.c_uint64, I, I]
@@ -250,10 +251,17 @@ class Lattice:
         return lib().orc_field(C.byref(self.p), _ptr(n))
 
     def local_energy(self, s: int, n=None) -> float:
+        return self.local_energy_abs(s, n)[0]
+
+    def local_energy_abs(self, s: int, n=None):
+        """(E_local, sum of |terms|) of site s with director n (FP64)."""
         if n is None:
             n = self.ni[s]
         n = np.asarray(n, np.float64)
-        return lib().orc_local_energy(C.byref(self.p), _ptr(self.ni), _ptr(self.pt), _ptr(self.ns), s, _ptr(n), None)
+        a = C.c_double()
+        e = lib().orc_local_energy(C.byref(self.p), _ptr(self.ni), _ptr(self.pt), _ptr(self.ns), s, _ptr(n),
+                                   C.byref(a))
+        return e, a.value
 
     def run_pass(self, T: float, ang_var: float, seed: int, stream: int, sweep: int, order: str, pass_: int,
                  flags: int = 0, tie_eps: float = 1e-5, feed: Optional[np.ndarray] = None, trace: bool = False):
@@ -284,6 +292,20 @@ class Lattice:
         lib().orc_measure(C.byref(self.p), _ptr(self.ni), _ptr(self.pt), _ptr(self.ns), _ptr(out))
         return dict(E=out[0], E_valid=out[1], Q=out[2:11].reshape(3, 3), S=out[11], director=out[12:15],
                     valid=int(out[15]))
+
+
+def propose(n, u0: float, u1: float, ang_var: float, flags: int = 0) -> np.ndarray:
+    """The rotated proposal of src/evolve.cpp:136-152 in FP64 (renormalised
+    unless F_NO_NORMALIZE)."""
+    n = np.ascontiguousarray(n, np.float32)
+    out = np.zeros(3)
+    lib().orc_propose(_ptr(n), u0, u1, ang_var, flags, _ptr(out))
+    return out
+
+
+def site_uniforms(site: int, seed: int, stream: int, sweep: int, tag: int = 0) -> np.ndarray:
+    r = philox([site, sweep & 0xFFFFFFFF, sweep >> 32, tag], [seed, stream])
+    return u24(r[:3])
 
 
 def adapt(ang_var: float, acc: int, valid: int) -> float:

@@ -119,9 +119,13 @@ def model_dict(model: Model) -> dict:
     return d
 
 
+def pool_run(md: dict, ops: Sequence[tuple], timeout: float = 300.0) -> List[Any]:
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(1) as pool:
+        return pool.apply_async(_worker, (md, list(ops))).get(timeout)
+
+
 def run(model: Model, ops: Sequence[tuple], timeout: float = 300.0) -> List[Any]:
     """Set up `model` in a fresh process with the reference's own code and run
     the ops (see _worker) there."""
-    ctx = mp.get_context("spawn")
-    with ctx.Pool(1) as pool:
-        return pool.apply_async(_worker, (model_dict(model), list(ops))).get(timeout)
+    return pool_run(model_dict(model), ops, timeout)

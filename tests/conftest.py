@@ -8,3 +8,7 @@ if ROOT not in sys.path:
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a GB300 (runs the CUDA engine)")
+
+PKG = os.path.join(ROOT, "mclics-backend_gb300")
+if PKG not in sys.path:
+    sys.path.insert(0, PKG)

@@ -1,0 +1,20 @@
+"""Shared test helpers: descriptors from oracle models, the GPU fixture."""
+import numpy as np
+
+import mcx
+from oracle import oracle as O
+
+
+def desc_from_model(m: O.Model, T=1.0, seed=1, stream=0, ang_var=0.5):
+    return mcx.replica(nx=m.nx, ny=m.ny, nz=m.nz, geometry=m.geometry, xbound=m.xbound, ybound=m.ybound,
+                       zbound=m.zbound, potential=m.potential, A=m.A, k11=m.k11, k22=m.k22, k33=m.k33, p0=m.p0,
+                       elecA=m.elecA, elecX=m.elecX, elecY=m.elecY, elecZ=m.elecZ, elecE=m.elecE, T=T,
+                       ang_var=ang_var, seed=seed, stream=stream,
+                       surfaces=[dict(anchoring=s.anchoring, W=s.W, theta_s=s.theta_s, phi_s=s.phi_s)
+                                 for s in m.surfaces], radius=m.radius)
+
+
+def random_state(m: O.Model, pt: np.ndarray, rng) -> np.ndarray:
+    ni = O.random_directors(m.n, rng)
+    ni[pt == 0] = (0, 0, 1)
+    return ni

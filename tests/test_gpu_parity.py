@@ -1,0 +1,223 @@
+"""Parity of the CUDA engine with the FP64 oracle, through the C ABI.
+
+Per red/black pass: every site's energy change matches the oracle's FP64
+evaluation of the same proposal within 1e-5 of the sum of |terms|; the
+proposal matches the oracle's FP64 rotation; accept/reject decisions are
+identical except where |u - exp(-dE/T)| <= 1e-5 (1 + exp(-dE/T)) (reported
+ties).  Measurements (E, Q, S) match within 2e-6 relative."""
+import numpy as np
+import pytest
+
+import mcx
+from oracle import oracle as O
+from helpers import desc_from_model, random_state
+
+pytestmark = pytest.mark.gpu
+
+TIE = 1e-5
+
+
+def _custom_model():
+    return O.Model(nx=8, ny=6, nz=6, geometry="custom", potential="ghrl", k11=1.0, k22=0.8, k33=1.2, p0=15,
+                   xbound="periodic", ybound="free", zbound="periodic",
+                   surfaces=[O.Surface("homeotropic_ghrl", 1.5), O.Surface("strong", 2.0, 30, 60),
+                             O.Surface("fg_ghrl", 1.0), O.Surface("rp_ghrl", 0.7, 45, 10)])
+
+
+def _custom_mask(m, rng):
+    pt = rng.choice([0, 1, 1, 1, 2, 3, 4, 5], size=m.n).astype(np.int32)
+    ns = O.random_directors(m.n, rng)
+    ns[pt < 2] = 0
+    return pt, ns
+
+
+CASES = {
+    "bulk_ll": O.Model(nx=16, ny=8, nz=6, potential="ll", A=1.0),
+    "bulk_ghrl_field": O.Model(nx=12, ny=10, nz=8, potential="ghrl", k11=1.0, k22=0.6, k33=1.4, p0=20, elecA=0.5,
+                               elecZ=1.0, elecX=0.3, elecE=1.5),
+    "slab_ghrl_padded": O.Model(nx=20, ny=6, nz=8, geometry="slab", potential="ghrl", k11=1.0, k22=0.8, k33=1.2,
+                                surfaces=[O.Surface("homeotropic", 4.0), O.Surface("homeotropic", 4.0)]),
+    "sphere_ghrl_fg_field": O.Model(nx=16, ny=16, nz=16, geometry="sphere", potential="ghrl", k11=1.0, k22=0.6,
+                                    k33=1.4, p0=20, elecA=0.3, elecZ=1.0, elecE=2.0, surfaces=[O.Surface("fg", 2.0)]),
+    "bulk_ll_free_padded": O.Model(nx=10, ny=6, nz=4, xbound="free", ybound="free", zbound="free", potential="ll",
+                                   A=1.3),
+    "sphere_ll_rp_radius": O.Model(nx=12, ny=12, nz=12, geometry="sphere", potential="ll", radius=4.5,
+                                   surfaces=[O.Surface("rp", 1.0, 60, 10)]),
+    "slab_ghrl_anch": O.Model(nx=8, ny=8, nz=6, geometry="slab", potential="ghrl", k11=1.48, k22=1.0, k33=2.28,
+                              surfaces=[O.Surface("fg_ghrl", 1.5), O.Surface("rp_ghrl", 2.0, 20, 70)]),
+    "custom_mixed": _custom_model(),
+    "bulk_ll_x_periodic_yz_free": O.Model(nx=14, ny=5, nz=3, xbound="periodic", ybound="free", zbound="free"),
+}
+
+
+def _setup(name, T=0.8, seed=77, stream=3, ang=0.6, rng_seed=0):
+    m = CASES[name]
+    rng = np.random.default_rng(rng_seed + sum(name.encode()))
+    eng = mcx.Engine([desc_from_model(m, T=T, seed=seed, stream=stream, ang_var=ang)])
+    if m.geometry == "custom":
+        pt, ns = _custom_mask(m, rng)
+        eng.set_mask(0, pt, ns)
+        lat = O.Lattice(m, pt=pt, ns=ns)
+    else:
+        lat = O.Lattice(m)
+        gpt, gns = eng.get_mask(0)
+        assert np.array_equal(gpt, lat.pt)
+        assert np.array_equal(gns, lat.ns)
+    ni0 = random_state(m, lat.pt, rng)
+    eng.set_state(0, ni0)
+    return m, lat, eng, ni0
+
+
+def _check_pass(m, lat, before, dE_g, acc_g, prop_g, after, T, ang, seed, stream, sweep, colour):
+    n = m.n
+    i = np.arange(n) % m.nx
+    j = (np.arange(n) // m.nx) % m.ny
+    k = np.arange(n) // (m.nx * m.ny)
+    upd = (((i + j + k) & 1) == colour) & (lat.pt != 0)
+    assert np.all(acc_g[~upd] == 255)
+    assert np.all(np.isin(acc_g[upd], [0, 1]))
+    lat.ni[:] = before
+    ties = 0
+    for s in np.nonzero(upd)[0]:
+        u = O.site_uniforms(int(s), seed, stream, sweep)
+        p64 = O.propose(before[s], u[0], u[1], ang)
+        assert np.max(np.abs(prop_g[s] - p64)) < 3e-6, (s, prop_g[s], p64)
+        e_new, a_new = lat.local_energy_abs(int(s), prop_g[s])
+        e_old, a_old = lat.local_energy_abs(int(s), before[s])
+        d64 = e_new - e_old
+        scale = a_new + a_old
+        assert abs(dE_g[s] - d64) <= 1e-5 * max(scale, 1e-3), (s, dE_g[s], d64, scale)
+        pa = np.exp(-d64 / T)
+        dec = u[2] < pa
+        if pa < 1 and abs(u[2] - pa) <= TIE * (1 + pa):
+            ties += 1
+            continue
+        assert bool(acc_g[s]) == dec, (s, dE_g[s], d64, u[2], pa)
+    want = before.copy()
+    acc_sites = np.nonzero(acc_g == 1)[0]
+    want[acc_sites] = prop_g[acc_sites]
+    assert np.array_equal(after, want)
+    return ties
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_pass_parity(name):
+    T, ang, seed, stream = 0.8, 0.6, 77, 3
+    m, lat, eng, ni0 = _setup(name, T, seed, stream, ang)
+    with eng:
+        for colour in (0, 1):
+            before = eng.get_state(0)
+            dE_g, acc_g, prop_g = eng.debug_pass(0, colour)
+            after = eng.get_state(0)
+            _check_pass(m, lat, before, dE_g, acc_g, prop_g, after, T, ang, seed, stream, 0, colour)
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_measure_parity(name):
+    m, lat, eng, ni0 = _setup(name)
+    with eng:
+        ni = ni0 * 0.5 + np.array([0.2, -0.1, 0.9], np.float32)
+        ni /= np.linalg.norm(ni, axis=1, keepdims=True)
+        ni[lat.pt == 0] = (0, 0, 1)
+        eng.set_state(0, ni)
+        lat.ni[:] = ni
+        g = eng.measure(0)
+        o = lat.measure()
+        assert g["valid"] == o["valid"]
+        assert g["E"] == pytest.approx(o["E"], rel=2e-6, abs=1e-6)
+        assert g["E_valid"] == pytest.approx(o["E_valid"], rel=2e-6, abs=1e-6)
+        assert np.allclose(g["Q"], o["Q"], atol=2e-6)
+        assert g["S"] == pytest.approx(o["S"], abs=2e-6)
+        assert abs(abs(np.dot(g["director"], o["director"])) - 1) < 1e-5
+
+
+@pytest.mark.parametrize("name", ["bulk_ll", "sphere_ghrl_fg_field", "custom_mixed", "slab_ghrl_padded"])
+def test_sweeps_and_step_rule_match_oracle(name):
+    """Three measured sweeps through the graph-free path: same states, same
+    step-size sequence, same running sums as the oracle's red/black sweeps."""
+    T, ang, seed, stream = 0.9, 0.5, 5, 1
+    m, lat, eng, ni0 = _setup(name, T, seed, stream, ang)
+    with eng:
+        lat.ni[:] = ni0
+        a = np.float32(ang)
+        S1 = E1 = 0.0
+        for sw in range(3):
+            eng.sweep(1, measure=True)
+            acc, a = lat.sweep(T, a, seed, stream, sw, "redblack")
+            r = lat.measure()
+            S1 += r["S"]
+            E1 += r["E"]
+            st = eng.stats(0)
+            assert np.float32(st[mcx.ST_ANG_VAR]) == np.float32(a)
+            assert st[mcx.ST_SWEEP_INDEX] == sw + 1
+        got = eng.get_state(0)
+        assert np.max(np.abs(got - lat.ni)) < 2e-5
+        st = eng.stats(0)
+        assert st[mcx.ST_N] == 3
+        assert st[mcx.ST_S1] == pytest.approx(S1, abs=1e-5)
+        assert st[mcx.ST_E1] == pytest.approx(E1, rel=1e-5)
+
+
+def test_graph_path_equals_direct_launches():
+    m = CASES["bulk_ghrl_field"]
+    rng = np.random.default_rng(9)
+    ni0 = random_state(m, np.ones(m.n, np.int32), rng)
+    d = desc_from_model(m, T=1.0, seed=3)
+    with mcx.Engine([d]) as a, mcx.Engine([d]) as b:
+        a.set_state(0, ni0)
+        b.set_state(0, ni0)
+        a.sweep(32, measure=True)
+        for _ in range(32):
+            b.sweep(1, measure=True)
+        assert np.array_equal(a.get_state(0), b.get_state(0))
+        sa, sb = a.stats(0), b.stats(0)
+        assert sa[mcx.ST_ANG_VAR] == sb[mcx.ST_ANG_VAR]
+        assert sa[mcx.ST_S1] == pytest.approx(sb[mcx.ST_S1], rel=1e-12)
+        assert a.kernel_launches > 0
+
+
+def test_batched_replicas_are_independent():
+    """Replicas of different sizes and geometries in one engine give exactly
+    what each gives alone."""
+    ms = [O.Model(nx=16, ny=16, nz=16, potential="ll"),
+          O.Model(nx=12, ny=10, nz=8, geometry="slab", potential="ll", surfaces=[O.Surface("homeotropic", 4.0)] * 2),
+          O.Model(nx=14, ny=14, nz=14, geometry="sphere", potential="ll", surfaces=[O.Surface("fg", 1.0)])]
+    descs = [desc_from_model(m, T=0.7 + 0.2 * q, seed=11, stream=q) for q, m in enumerate(ms)]
+    rng = np.random.default_rng(2)
+    states = [random_state(m, O.Lattice(m).pt, rng) for m in ms]
+    with mcx.Engine(descs) as eng:
+        for q in range(3):
+            eng.set_state(q, states[q])
+        eng.sweep(20, measure=True)
+        batched = [eng.get_state(q) for q in range(3)]
+        bstats = [eng.stats(q) for q in range(3)]
+    for q in range(3):
+        with mcx.Engine([descs[q]]) as one:
+            one.set_state(0, states[q])
+            one.sweep(20, measure=True)
+            assert np.array_equal(one.get_state(0), batched[q])
+            assert one.stats(0)[mcx.ST_S1] == pytest.approx(bstats[q][mcx.ST_S1], rel=1e-12)
+
+
+def test_equilibrium_sanity_ll():
+    m = O.Model(nx=16, ny=16, nz=16)
+    with mcx.Engine([desc_from_model(m, T=0.4, seed=1, stream=0), desc_from_model(m, T=2.0, seed=1, stream=1)]) as e:
+        e.init_random(0, 1)
+        e.init_random(1, 2)
+        e.sweep(400)
+        e.sweep(100, measure=True)
+        cold, hot = e.stats(0), e.stats(1)
+        assert cold[mcx.ST_S1] / 100 > 0.85
+        assert hot[mcx.ST_S1] / 100 < 0.15
+        assert cold[mcx.ST_E1] / 100 < -7.0  # ground state -9
+
+
+def test_errors_are_status_codes():
+    with pytest.raises(mcx.McxError) as ei:
+        mcx.Engine([mcx.replica(nx=15)])
+    assert ei.value.status == 4
+    with mcx.Engine([mcx.replica(nx=8, ny=8, nz=8)]) as e:
+        with pytest.raises(mcx.McxError):
+            e.get_state(3)
+        with pytest.raises(mcx.McxError):
+            e.set_field(1.0)
