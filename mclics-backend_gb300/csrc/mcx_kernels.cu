@@ -182,17 +182,19 @@ __device__ __forceinline__ float bonds_delta(const RepDev &R, float n0x, float n
     for (int d = 0; d < 6; d++) {
       const float dn = n0x * nb[d][0] + n0y * nb[d][1] + n0z * nb[d][2];
       const float dp = px * nb[d][0] + py * nb[d][1] + pz * nb[d][2];
-      acc += w[d] * ((dp - dn) * (dp + dn));
+      // the 0/1 weight multiplies one factor exactly, so masked and unmasked
+      // specialisations round identically
+      acc = fmaf((dp - dn) * w[d], dp + dn, acc);
     }
     return -1.5f * R.A * acc;
   } else {
     float acc = 0.f;
-    acc += w[0] * (bond<POT, 0>(R, px, py, pz, nb[0]) - bond<POT, 0>(R, n0x, n0y, n0z, nb[0]));
-    acc += w[1] * (bond<POT, 1>(R, px, py, pz, nb[1]) - bond<POT, 1>(R, n0x, n0y, n0z, nb[1]));
-    acc += w[2] * (bond<POT, 2>(R, px, py, pz, nb[2]) - bond<POT, 2>(R, n0x, n0y, n0z, nb[2]));
-    acc += w[3] * (bond<POT, 3>(R, px, py, pz, nb[3]) - bond<POT, 3>(R, n0x, n0y, n0z, nb[3]));
-    acc += w[4] * (bond<POT, 4>(R, px, py, pz, nb[4]) - bond<POT, 4>(R, n0x, n0y, n0z, nb[4]));
-    acc += w[5] * (bond<POT, 5>(R, px, py, pz, nb[5]) - bond<POT, 5>(R, n0x, n0y, n0z, nb[5]));
+    acc = fmaf(w[0], bond<POT, 0>(R, px, py, pz, nb[0]) - bond<POT, 0>(R, n0x, n0y, n0z, nb[0]), acc);
+    acc = fmaf(w[1], bond<POT, 1>(R, px, py, pz, nb[1]) - bond<POT, 1>(R, n0x, n0y, n0z, nb[1]), acc);
+    acc = fmaf(w[2], bond<POT, 2>(R, px, py, pz, nb[2]) - bond<POT, 2>(R, n0x, n0y, n0z, nb[2]), acc);
+    acc = fmaf(w[3], bond<POT, 3>(R, px, py, pz, nb[3]) - bond<POT, 3>(R, n0x, n0y, n0z, nb[3]), acc);
+    acc = fmaf(w[4], bond<POT, 4>(R, px, py, pz, nb[4]) - bond<POT, 4>(R, n0x, n0y, n0z, nb[4]), acc);
+    acc = fmaf(w[5], bond<POT, 5>(R, px, py, pz, nb[5]) - bond<POT, 5>(R, n0x, n0y, n0z, nb[5]), acc);
     return acc;
   }
 }

@@ -172,6 +172,8 @@ class Engine:
         self.close()
 
     def sites(self, r: int) -> int:
+        if not 0 <= r < self.n:
+            raise McxError(1, f"replica {r} out of range [0, {self.n})")
         d = self.descs[r]
         return d.nx * d.ny * d.nz
 
