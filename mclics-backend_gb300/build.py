@@ -12,7 +12,8 @@ from concurrent.futures import ThreadPoolExecutor
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "csrc")
-OUT = os.path.join(HERE, "_build")
+OUT = os.environ.get("MCX_BUILD_DIR", os.path.join(HERE, "_build"))
+EXTRA = os.environ.get("MCX_NVCC_FLAGS", "").split()
 NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 HOSTFLAGS = ["-fPIC", "-ffp-contract=off", "-O3", "-fno-strict-aliasing"]
@@ -49,7 +50,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
         if not force and _newer(obj, [src] + headers):
             continue
         if tu.endswith(".cu"):
-            cmd = [NVCC, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xptxas", "-v", "-Xcompiler",
+            cmd = [NVCC, *ARCH, *EXTRA, "-O3", "-lineinfo", "-std=c++17", "-Xptxas", "-v", "-Xcompiler",
                    ",".join(HOSTFLAGS), "-c", src, "-o", obj]
         else:
             cmd = ["g++", "-std=c++17", *HOSTFLAGS, "-I", os.environ.get("CUDA_INC", "/usr/local/cuda/include"),

@@ -15,7 +15,9 @@
 namespace mcx {
 
 constexpr int kMaxSurf = 16;
-constexpr int kBlock = 128;  // threads per CTA of the sweep / measure kernels
+constexpr int kBlock = 256;  // threads per CTA of the pass kernels: one site each
+constexpr int kLanes = 8;    // atomic lanes per replica (spreads same-address atomics)
+constexpr int kQ = 7;        // measured sums: E_all, E_valid, n_a n_b for xx xy xz yy yz
 
 enum : int { POT_LL = 0, POT_GHRL = 1 };
 enum : int { BOUND_FREE = 0, BOUND_PERIODIC = 1 };
@@ -30,22 +32,26 @@ enum : int {
   ANCH_STRONG_GHRL = 7
 };
 // Philox counter word 3: which stream of uniforms.
-enum : uint32_t { TAG_PLAIN = 0u, TAG_VMF = 1u, TAG_IC = 0x1C000000u };
+// The pass colour is or-ed into the low bit.
+enum : uint32_t { TAG_PLAIN = 0u, TAG_VMF = 2u, TAG_IC = 0x1C000000u };
 
 // Per-replica constants, resident in device memory (read-only in kernels).
 struct RepDev {
   int nx, ny, nz;
-  int hx, hs, g4;  // half-row length, padded stride, float4 groups per row
+  int hx, hs;  // half-row length, padded row stride (a multiple of 4)
   int xb, yb, zb;
   int nsurf;
   int valid;  // active sites
   int ntot;   // nx*ny*nz
-  int pad0;
-  long long plane;    // elements per (colour, component) plane
+  int hp;     // same-colour site pairs per row, (hx + 1) / 2
+  int npair;  // pairs per colour, hp*ny*nz: one thread each
+  int plane;  // elements per (colour, component) plane, hs*ny*nz
+  int ncta;   // CTAs of this replica in one pass launch
+  uint32_t hp_m, ny_m;  // n / hp == (n * hp_m) >> hp_p for n < 2^31
+  int hp_p, ny_p;
   long long dir_off;  // float offset of this replica's [2][3][plane] block
   long long pt_off;   // byte offset of its [2][plane] point types
   long long ns_off;   // float offset of its [2][3][plane] normals
-  long long ngroups;  // float4 groups per colour = g4*ny*nz
   float A, elecA, elecE, ex, ey, ez;
   float lam, mu, nu, rho, sigma;
   uint32_t seed, stream;
@@ -58,16 +64,19 @@ struct RepDev {
 struct RepState {
   float T;
   float ang_var;
-  unsigned int acc;          // accepted moves of the sweep in progress
+  unsigned long long sweep;  // sweeps done: the RNG counter
+  unsigned long long meas;   // measured sweeps done: the ring-slot counter
+  unsigned int acc[kLanes];  // accepted moves of the sweep in progress, by lane
+  unsigned int done;         // CTAs of the running colour-1 pass that finished
   unsigned int pad;
-  unsigned long long sweep;  // RNG counter: sweeps done
 };
 
 // Running sums (doubles), indexed by the MCX_ST_* layout of mcx.h.
 constexpr int kStats = 16;
-// Measurement accumulators: E_all, E_valid, then sum n_a n_b for
-// xx, xy, xz, yy, yz, zz.
-constexpr int kMacc = 8;
+
+__host__ __device__ __forceinline__ uint32_t fastdiv(uint32_t n, uint32_t m, int p) {
+  return (uint32_t)(((unsigned long long)n * m) >> p);
+}
 
 // ---------------------------------------------------------------------------
 // Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11).
@@ -98,6 +107,19 @@ __host__ __device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint32_t k0, ui
 
 // 24-bit uniform on [0, 1), exact in float.
 __host__ __device__ __forceinline__ float u01(uint32_t x) { return (float)(x >> 8) * 5.9604644775390625e-8f; }
+
+// The six 21-bit uniforms of one Philox draw, for the even (A) and odd (B)
+// site of a same-colour pair: A takes the top 21 bits of words 0, 1, 2; B the
+// top 21 bits of word 3 and the low bits of words 0|1 and 2|3.
+__host__ __device__ __forceinline__ void pair_uniforms(uint4 w, float uA[3], float uB[3]) {
+  const float sc = 4.76837158203125e-7f;  // 2^-21
+  uA[0] = (float)(w.x >> 11) * sc;
+  uA[1] = (float)(w.y >> 11) * sc;
+  uA[2] = (float)(w.z >> 11) * sc;
+  uB[0] = (float)(w.w >> 11) * sc;
+  uB[1] = (float)(((w.x & 0x7FFu) << 10) | (w.y & 0x3FFu)) * sc;
+  uB[2] = (float)(((w.z & 0x7FFu) << 10) | (w.w & 0x3FFu)) * sc;
+}
 
 // ---------------------------------------------------------------------------
 // Energies.  Neighbour slots follow the reference order x+, x-, y+, y-, z+,

@@ -19,7 +19,8 @@
 using namespace mcx;
 
 namespace {
-constexpr int kChunk = 16;  // sweeps per captured graph
+constexpr int kChunk = 16;     // sweeps per captured graph
+constexpr int kRingCap = 512;  // measured sweeps buffered before the statistics are folded
 std::string g_last_error;
 }  // namespace
 
@@ -38,16 +39,18 @@ struct mcx_engine {
   uint8_t *d_pt = nullptr;
   float *d_ns = nullptr;
   RepState *d_st = nullptr;
-  double *d_macc = nullptr;
   double *d_stats = nullptr;
+  double *d_ring = nullptr;  // [nrep][ring_cap + 1][kLanes][kQ]
+  int ring_cap = kRingCap;
+  unsigned long long meas_flushed = 0;  // measured sweeps already folded into the stats
+  int pending = 0;                      // measured sweeps waiting in the ring
   double *d_series = nullptr;
-  double *d_mout = nullptr;
   int series_cap = 0;
+  double *d_mout = nullptr;
   float *d_stage = nullptr;  // AoS staging, 3 * max sites floats
   int *d_stage_pt = nullptr;
   long long max_sites = 0;
   cudaGraphExec_t graph[2] = {nullptr, nullptr};  // [measure]
-  int graph_nodes[2] = {0, 0};
   long long launches = 0;
   std::string err;
 };
@@ -77,6 +80,15 @@ static mcx_status fail(mcx_engine *e, mcx_status st, const char *fmt, ...) {
 
 static long long align_up(long long x, long long a) { return (x + a - 1) / a * a; }
 
+// n / d == (n * m) >> p for every n < 2^31 with p = 31 + ceil(log2 d) and
+// m = ceil(2^p / d), which fits in 32 bits (Granlund & Montgomery, PLDI'94).
+static void div_magic(uint32_t d, uint32_t &m, int &p) {
+  int L = 0;
+  while ((1ull << L) < d) L++;
+  p = 31 + L;
+  m = (uint32_t)(((1ull << p) + d - 1) / d);
+}
+
 extern "C" int mcx_version(void) { return 1; }
 
 extern "C" const char *mcx_last_error(const mcx_engine *e) { return e ? e->err.c_str() : g_last_error.c_str(); }
@@ -95,7 +107,7 @@ static void free_engine(mcx_engine *e) {
   cudaFree(e->d_pt);
   cudaFree(e->d_ns);
   cudaFree(e->d_st);
-  cudaFree(e->d_macc);
+  cudaFree(e->d_ring);
   cudaFree(e->d_stats);
   cudaFree(e->d_series);
   cudaFree(e->d_mout);
@@ -160,18 +172,20 @@ extern "C" mcx_status mcx_create(int n, const mcx_replica_desc *descs, mcx_engin
     R.nz = d.nz;
     R.hx = d.nx / 2;
     R.hs = (int)align_up(R.hx, 4);
-    R.g4 = R.hs / 4;
     R.xb = d.xbound;
     R.yb = d.ybound;
     R.zb = d.zbound;
     R.nsurf = d.n_surfaces;
     R.ntot = d.nx * d.ny * d.nz;
-    R.plane = (long long)R.hs * d.ny * d.nz;
-    R.ngroups = (long long)R.g4 * d.ny * d.nz;
+    R.plane = R.hs * d.ny * d.nz;
+    R.hp = (R.hx + 1) / 2;
+    R.npair = R.hp * d.ny * d.nz;
+    div_magic((uint32_t)R.hp, R.hp_m, R.hp_p);
+    div_magic((uint32_t)d.ny, R.ny_m, R.ny_p);
     R.dir_off = dir_total;
-    dir_total += align_up(6 * R.plane, 64);
+    dir_total += align_up(6LL * R.plane, 64);
     R.pt_off = pt_total;
-    pt_total += align_up(2 * R.plane, 256);
+    pt_total += align_up(2LL * R.plane, 256);
     R.A = d.A;
     R.elecA = d.elecA;
     R.elecE = d.elecE;
@@ -199,7 +213,11 @@ extern "C" mcx_status mcx_create(int n, const mcx_replica_desc *descs, mcx_engin
     if (d.geometry != MCX_GEO_BULK) e->var.mask = true;
     if (d.elecA != 0.f) e->var.field = true;
     e->max_sites = std::max(e->max_sites, (long long)R.ntot);
-    for (long long b = 0; b < R.ngroups; b += kBlock) e->map.push_back(make_int2(r, (int)b));
+    R.ncta = 0;
+    for (long long b = 0; b < R.npair; b += kBlock) {
+      e->map.push_back(make_int2(r, (int)b));
+      R.ncta++;
+    }
   }
   for (int r = 0; r < n; r++) e->rep[r].ns_off = e->var.mask ? e->rep[r].dir_off : -1;
   mcx_status st = MCX_OK;
@@ -225,8 +243,9 @@ extern "C" mcx_status mcx_create(int n, const mcx_replica_desc *descs, mcx_engin
   CKC(cudaMalloc(&e->d_rep, sizeof(RepDev) * n));
   CKC(cudaMalloc(&e->d_map, sizeof(int2) * e->map.size()));
   CKC(cudaMalloc(&e->d_st, sizeof(RepState) * n));
-  CKC(cudaMalloc(&e->d_macc, sizeof(double) * kMacc * n));
-  CKC(cudaMemsetAsync(e->d_macc, 0, sizeof(double) * kMacc * n, e->stream));
+  const size_t ring_n = (size_t)n * (e->ring_cap + 1) * kLanes * kQ;
+  CKC(cudaMalloc(&e->d_ring, sizeof(double) * ring_n));
+  CKC(cudaMemsetAsync(e->d_ring, 0, sizeof(double) * ring_n, e->stream));
   CKC(cudaMalloc(&e->d_stats, sizeof(double) * kStats * n));
   CKC(cudaMemsetAsync(e->d_stats, 0, sizeof(double) * kStats * n, e->stream));
   CKC(cudaMalloc(&e->d_mout, sizeof(double) * 16 * n));
@@ -246,11 +265,9 @@ extern "C" mcx_status mcx_create(int n, const mcx_replica_desc *descs, mcx_engin
   CKC(cudaMemcpyAsync(e->d_rep, e->rep.data(), sizeof(RepDev) * n, cudaMemcpyHostToDevice, e->stream));
   std::vector<RepState> hs(n);
   for (int r = 0; r < n; r++) {
+    memset(&hs[r], 0, sizeof(RepState));
     hs[r].T = e->desc[r].T;
     hs[r].ang_var = e->desc[r].ang_var > 0 ? e->desc[r].ang_var : 0.5f;
-    hs[r].acc = 0;
-    hs[r].pad = 0;
-    hs[r].sweep = 0;
   }
   CKC(cudaMemcpyAsync(e->d_st, hs.data(), sizeof(RepState) * n, cudaMemcpyHostToDevice, e->stream));
   CKC(cudaStreamSynchronize(e->stream));
@@ -419,8 +436,7 @@ extern "C" mcx_status mcx_set_step(mcx_engine *e, int r, float a) {
   return set_scalar(e, r, offsetof(RepState, ang_var), a, false);
 }
 
-// One sweep's kernels on e->stream.
-static void enqueue_sweep(mcx_engine *e, bool measure) {
+static PassArgs pass_args(mcx_engine *e) {
   PassArgs pa{};
   pa.reps = e->d_rep;
   pa.map = e->d_map;
@@ -428,17 +444,20 @@ static void enqueue_sweep(mcx_engine *e, bool measure) {
   pa.pt = e->d_pt;
   pa.ns = e->d_ns;
   pa.st = e->d_st;
+  pa.stats = e->d_stats;
+  pa.ring = e->d_ring;
+  pa.ring_cap = e->ring_cap;
+  return pa;
+}
+
+// One sweep's kernels on e->stream: the two colours.
+static void enqueue_sweep(mcx_engine *e, bool measure) {
+  PassArgs pa = pass_args(e);
   const int nb = (int)e->map.size();
   for (int c = 0; c < 2; c++) {
     pa.colour = c;
-    launch_pass(e->var, pa, nb, false, e->stream);
+    launch_pass(e->var, measure ? MODE_SWEEP_MEASURE : MODE_SWEEP, pa, nb, e->stream);
   }
-  EpilogueArgs ea{e->d_rep, e->d_st, e->d_macc, e->d_stats, e->d_series, e->series_cap, e->nrep};
-  if (measure) {
-    MeasureArgs ma{e->d_rep, e->d_map, e->d_dir, e->d_pt, e->d_ns, e->d_macc};
-    launch_measure(e->var, ma, nb, e->stream);
-  }
-  launch_epilogue(ea, measure, e->stream);
 }
 
 static mcx_status build_graph(mcx_engine *e, int measure) {
@@ -452,28 +471,51 @@ static mcx_status build_graph(mcx_engine *e, int measure) {
   r = cudaGraphInstantiate(&e->graph[measure], g, 0);
   cudaGraphDestroy(g);
   if (r != cudaSuccess) return fail(e, MCX_ERR_CUDA, "cudaGraphInstantiate: %s", cudaGetErrorString(r));
-  e->graph_nodes[measure] = kChunk * (measure ? 4 : 3);
   return MCX_OK;
 }
 
-extern "C" mcx_status mcx_sweep(mcx_engine *e, int n, int measure) {
-  if (!e) return fail(nullptr, MCX_ERR_INVALID, "null engine");
-  if (n < 0) return fail(e, MCX_ERR_INVALID, "negative sweep count");
-  const int m = measure ? 1 : 0;
+// Folds the measured sweeps waiting in the ring into the running sums.
+static mcx_status flush(mcx_engine *e) {
+  if (e->pending == 0) return MCX_OK;
+  FlushArgs f{e->d_rep, e->d_ring, e->ring_cap, e->d_stats, e->d_series, e->series_cap, e->meas_flushed, e->pending};
+  launch_flush(f, e->nrep, e->stream);
+  e->launches += 1;
+  CKL(e);
+  e->meas_flushed += (unsigned long long)e->pending;
+  e->pending = 0;
+  return MCX_OK;
+}
+
+static mcx_status run_sweeps(mcx_engine *e, int n, int m) {
   if (n >= kChunk && !e->graph[m]) {
     if (mcx_status st = build_graph(e, m)) return st;
   }
   int done = 0;
   while (n - done >= kChunk) {
     CK(e, cudaGraphLaunch(e->graph[m], e->stream));
-    e->launches += e->graph_nodes[m];
+    e->launches += 2 * kChunk;
     done += kChunk;
   }
   for (; done < n; done++) {
     enqueue_sweep(e, m != 0);
-    e->launches += m ? 4 : 3;
+    e->launches += 2;
   }
   CKL(e);
+  return MCX_OK;
+}
+
+extern "C" mcx_status mcx_sweep(mcx_engine *e, int n, int measure) {
+  if (!e) return fail(nullptr, MCX_ERR_INVALID, "null engine");
+  if (n < 0) return fail(e, MCX_ERR_INVALID, "negative sweep count");
+  if (!measure) return run_sweeps(e, n, 0);
+  while (n > 0) {
+    const int chunk = std::min(n, e->ring_cap - e->pending);
+    if (mcx_status st = run_sweeps(e, chunk, 1)) return st;
+    e->pending += chunk;
+    n -= chunk;
+    if (e->pending == e->ring_cap)
+      if (mcx_status st = flush(e)) return st;
+  }
   return MCX_OK;
 }
 
@@ -486,11 +528,13 @@ extern "C" mcx_status mcx_sync(mcx_engine *e) {
 extern "C" mcx_status mcx_measure(mcx_engine *e, int r, double *out) {
   if (mcx_status st = check_rep(e, r)) return st;
   if (!out) return fail(e, MCX_ERR_INVALID, "null output");
-  MeasureArgs ma{e->d_rep, e->d_map, e->d_dir, e->d_pt, e->d_ns, e->d_macc};
-  launch_measure(e->var, ma, (int)e->map.size(), e->stream);
-  EpilogueArgs ea{e->d_rep, e->d_st, e->d_macc, e->d_stats, e->d_series, e->series_cap, e->nrep};
-  launch_measure_out(ea, e->d_mout, e->stream);
-  e->launches += 2;
+  PassArgs pa = pass_args(e);
+  for (int c = 0; c < 2; c++) {
+    pa.colour = c;
+    launch_pass(e->var, MODE_MEASURE_ONLY, pa, (int)e->map.size(), e->stream);
+  }
+  launch_measure_out(e->d_rep, e->d_ring, e->ring_cap, e->nrep, e->d_mout, e->stream);
+  e->launches += 3;
   CKL(e);
   CK(e, cudaMemcpyAsync(out, e->d_mout + (size_t)r * 16, sizeof(double) * 16, cudaMemcpyDeviceToHost, e->stream));
   CK(e, cudaStreamSynchronize(e->stream));
@@ -500,6 +544,7 @@ extern "C" mcx_status mcx_measure(mcx_engine *e, int r, double *out) {
 extern "C" mcx_status mcx_get_stats(mcx_engine *e, int r, double *out) {
   if (mcx_status st = check_rep(e, r)) return st;
   if (!out) return fail(e, MCX_ERR_INVALID, "null output");
+  if (mcx_status st = flush(e)) return st;
   CK(e, cudaMemcpyAsync(out, e->d_stats + (size_t)r * kStats, sizeof(double) * kStats, cudaMemcpyDeviceToHost,
                         e->stream));
   CK(e, cudaStreamSynchronize(e->stream));
@@ -510,6 +555,7 @@ extern "C" mcx_status mcx_reset_stats(mcx_engine *e, int r) {
   if (!e) return fail(nullptr, MCX_ERR_INVALID, "null engine");
   const int r0 = r < 0 ? 0 : r, r1 = r < 0 ? e->nrep : r + 1;
   if (r >= e->nrep) return fail(e, MCX_ERR_INVALID, "replica %d out of range", r);
+  if (mcx_status st = flush(e)) return st;
   // keep the step size and sweep index entries (11, 12), clear the sums
   for (int q = r0; q < r1; q++)
     CK(e, cudaMemsetAsync(e->d_stats + (size_t)q * kStats, 0, sizeof(double) * 11, e->stream));
@@ -520,6 +566,7 @@ extern "C" mcx_status mcx_reset_stats(mcx_engine *e, int r) {
 extern "C" mcx_status mcx_set_series(mcx_engine *e, int cap) {
   if (!e) return fail(nullptr, MCX_ERR_INVALID, "null engine");
   if (cap < 0) return fail(e, MCX_ERR_INVALID, "negative series capacity");
+  if (mcx_status st = flush(e)) return st;
   CK(e, cudaStreamSynchronize(e->stream));
   cudaFree(e->d_series);
   e->d_series = nullptr;
@@ -530,12 +577,6 @@ extern "C" mcx_status mcx_set_series(mcx_engine *e, int cap) {
     CK(e, cudaMemset(e->d_series, 0, sizeof(double) * 2 * (size_t)cap * e->nrep));
     e->series_cap = cap;
   }
-  // the captured graphs hold the old series pointer
-  for (int m = 0; m < 2; m++)
-    if (e->graph[m]) {
-      cudaGraphExecDestroy(e->graph[m]);
-      e->graph[m] = nullptr;
-    }
   return MCX_OK;
 }
 
@@ -543,13 +584,13 @@ extern "C" mcx_status mcx_get_series(mcx_engine *e, int r, int count, double *ou
   if (mcx_status st = check_rep(e, r)) return st;
   if (!out || count < 0) return fail(e, MCX_ERR_INVALID, "bad series request");
   if (count > e->series_cap) return fail(e, MCX_ERR_INVALID, "count %d exceeds series capacity %d", count, e->series_cap);
-  double st[kStats];
-  if (mcx_status s = mcx_get_stats(e, r, st)) return s;
-  const long long n = (long long)st[0];
+  if (mcx_status st = flush(e)) return st;
+  const long long n = (long long)e->meas_flushed;
   if (count > n) return fail(e, MCX_ERR_INVALID, "only %lld measured sweeps recorded", n);
   std::vector<double> ring(2 * (size_t)e->series_cap);
-  CK(e, cudaMemcpy(ring.data(), e->d_series + (size_t)r * e->series_cap * 2, sizeof(double) * ring.size(),
-                   cudaMemcpyDeviceToHost));
+  CK(e, cudaMemcpyAsync(ring.data(), e->d_series + (size_t)r * e->series_cap * 2, sizeof(double) * ring.size(),
+                        cudaMemcpyDeviceToHost, e->stream));
+  CK(e, cudaStreamSynchronize(e->stream));
   for (int q = 0; q < count; q++) {
     const long long idx = (n - count + q) % e->series_cap;
     out[2 * q] = ring[2 * idx];
@@ -565,25 +606,16 @@ extern "C" mcx_status mcx_pass_timing(mcx_engine *e, int n, float *pass_ms, floa
   if (n <= 0) return fail(e, MCX_ERR_INVALID, "need n_sweeps > 0");
   std::vector<cudaEvent_t> ev(4 * (size_t)n);
   for (auto &x : ev) CK(e, cudaEventCreate(&x));
-  PassArgs pa{};
-  pa.reps = e->d_rep;
-  pa.map = e->d_map;
-  pa.dir = e->d_dir;
-  pa.pt = e->d_pt;
-  pa.ns = e->d_ns;
-  pa.st = e->d_st;
+  PassArgs pa = pass_args(e);
   const int nb = (int)e->map.size();
-  EpilogueArgs ea{e->d_rep, e->d_st, e->d_macc, e->d_stats, e->d_series, e->series_cap, e->nrep};
-  for (int s = 0; s < n; s++) {
+  for (int s = 0; s < n; s++)
     for (int c = 0; c < 2; c++) {
       pa.colour = c;
       CK(e, cudaEventRecord(ev[4 * s + 2 * c], e->stream));
-      launch_pass(e->var, pa, nb, false, e->stream);
+      launch_pass(e->var, MODE_SWEEP, pa, nb, e->stream);
       CK(e, cudaEventRecord(ev[4 * s + 2 * c + 1], e->stream));
     }
-    launch_epilogue(ea, false, e->stream);
-  }
-  e->launches += 3LL * n;
+  e->launches += 2LL * n;
   CKL(e);
   CK(e, cudaStreamSynchronize(e->stream));
   float sum = 0.f, t;
@@ -645,22 +677,15 @@ extern "C" mcx_status mcx_debug_pass(mcx_engine *e, int r, int colour, float *dE
   CK(e, cudaMemsetAsync(d_prop, 0, sizeof(float) * 3 * R.ntot, e->stream));
   CK(e, cudaMemsetAsync(d_acc, 0xFF, R.ntot, e->stream));
   CK(e, cudaMemcpyAsync(d_map, sub.data(), sizeof(int2) * sub.size(), cudaMemcpyHostToDevice, e->stream));
-  PassArgs pa{};
-  pa.reps = e->d_rep;
+  PassArgs pa = pass_args(e);
   pa.map = d_map;
-  pa.dir = e->d_dir;
-  pa.pt = e->d_pt;
-  pa.ns = e->d_ns;
-  pa.st = e->d_st;
   pa.colour = colour;
   pa.tr_dE = d_dE;
   pa.tr_acc = d_acc;
   pa.tr_prop = d_prop;
-  launch_pass(e->var, pa, (int)sub.size(), true, e->stream);
+  launch_pass(e->var, MODE_TRACE, pa, (int)sub.size(), e->stream);
   e->launches += 1;
   CKL(e);
-  // a trace pass does not count toward the step-size rule
-  CK(e, cudaMemsetAsync(&e->d_st[r].acc, 0, sizeof(unsigned), e->stream));
   if (dE) CK(e, cudaMemcpyAsync(dE, d_dE, sizeof(float) * R.ntot, cudaMemcpyDeviceToHost, e->stream));
   if (acc) CK(e, cudaMemcpyAsync(acc, d_acc, R.ntot, cudaMemcpyDeviceToHost, e->stream));
   if (prop) CK(e, cudaMemcpyAsync(prop, d_prop, sizeof(float) * 3 * R.ntot, cudaMemcpyDeviceToHost, e->stream));

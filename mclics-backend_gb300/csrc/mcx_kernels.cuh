@@ -9,53 +9,54 @@
 
 namespace mcx {
 
-// Which specialisation of the sweep / measure kernels a batch runs: the pair
-// potential, whether any replica has a mask (inactive or surface sites), and
-// whether any replica has a field term.  Fixed per engine.
+// Which specialisation of the pass kernel a batch runs: the pair potential,
+// whether any replica has a mask (inactive or surface sites), and whether any
+// replica has a field term.  Fixed per engine.
 struct Variant {
   int pot;
   bool mask;
   bool field;
 };
 
+// What a pass launch does.
+enum PassMode : int {
+  MODE_SWEEP = 0,         // update one colour; colour 1 ends the sweep
+  MODE_SWEEP_MEASURE = 1, // the same, and add E / Q of the final state to the sweep's ring slot
+  MODE_MEASURE_ONLY = 2,  // no update: E / Q of the current state into the extra ring slot
+  MODE_TRACE = 3          // update one colour of one replica and record every site
+};
+
 struct PassArgs {
   const RepDev *reps;
-  const int2 *map;  // per CTA: (replica, first float4 group)
+  const int2 *map;  // per CTA: (replica, first site of the colour)
   float *dir;
   const uint8_t *pt;
   const float *ns;
   RepState *st;
+  double *stats;  // [nrep][kStats]
+  double *ring;   // [nrep][ring_cap + 1][kLanes][kQ]
+  int ring_cap;
   int colour;
-  // trace outputs (natural site order of one replica), used only by the
-  // trace specialisation
+  // trace outputs (natural site order of one replica)
   float *tr_dE;
   uint8_t *tr_acc;
   float *tr_prop;
 };
 
-struct MeasureArgs {
+struct FlushArgs {
   const RepDev *reps;
-  const int2 *map;
-  const float *dir;
-  const uint8_t *pt;
-  const float *ns;
-  double *macc;  // [nrep][kMacc]
-};
-
-struct EpilogueArgs {
-  const RepDev *reps;
-  RepState *st;
-  double *macc;
-  double *stats;   // [nrep][kStats]
+  double *ring;
+  int ring_cap;
+  double *stats;
   double *series;  // [nrep][series_cap][2] or null
   int series_cap;
-  int nrep;
+  unsigned long long first;  // measured-sweep index of the first pending slot
+  int count;                 // pending slots
 };
 
-void launch_pass(const Variant &v, const PassArgs &a, int nblocks, bool trace, cudaStream_t st);
-void launch_measure(const Variant &v, const MeasureArgs &a, int nblocks, cudaStream_t st);
-void launch_epilogue(const EpilogueArgs &a, bool measure, cudaStream_t st);
-void launch_measure_out(const EpilogueArgs &a, double *out, cudaStream_t st);
+void launch_pass(const Variant &v, int mode, const PassArgs &a, int nblocks, cudaStream_t st);
+void launch_flush(const FlushArgs &f, int nrep, cudaStream_t st);
+void launch_measure_out(const RepDev *reps, double *ring, int ring_cap, int nrep, double *out, cudaStream_t st);
 void launch_aos_to_split(const RepDev &R, const float *aos, float *dir, cudaStream_t st);
 void launch_split_to_aos(const RepDev &R, const float *dir, float *aos, cudaStream_t st);
 void launch_mask_to_split(const RepDev &R, const int *pt_aos, const float *ns_aos, uint8_t *pt, float *ns,

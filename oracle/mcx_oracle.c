@@ -52,8 +52,41 @@ void orc_philox(const uint32_t ctr_in[4], const uint32_t key_in[2], uint32_t out
   out[3] = c3;
 }
 
-/* 24-bit uniform on [0,1): exactly representable in float and double. */
-static double u24(uint32_t x) { return (double)(x >> 8) * (1.0 / 16777216.0); }
+/* The three uniforms of one site update.  Same-colour sites are paired along
+ * x: site i of colour c = (i+j+k)%2 in row (j,k) has colour-row position
+ * h = i/2, and positions 2q, 2q+1 form pair q.  One Philox4x32-10 draw per
+ * pair, counter (row*pairs_per_row + q, sweep_lo, sweep_hi, tag | c), key
+ * (seed, stream), gives 128 bits = six 21-bit uniforms: the even position
+ * takes the top 21 bits of words 0, 1, 2; the odd one the top 21 bits of
+ * word 3 and the low bits of words 0|1 and 2|3.  Multiples of 2^-21 are
+ * exact in float and double. */
+void orc_site_uniforms(int nx, int ny, long s, uint32_t seed, uint32_t stream, uint64_t sweep, uint32_t tag,
+                       double u[3]) {
+  int i = (int)(s % nx);
+  long row = s / nx;
+  int j = (int)(row % ny), k = (int)(row / ny);
+  int c = (i + j + k) & 1;
+  int hx = (nx + 1) / 2;
+  int hp = (hx + 1) / 2;
+  int h = i >> 1;
+  uint32_t ctr[4] = {(uint32_t)(row * hp + (h >> 1)), (uint32_t)sweep, (uint32_t)(sweep >> 32), tag | (uint32_t)c};
+  uint32_t key[2] = {seed, stream}, w[4];
+  orc_philox(ctr, key, w);
+  uint32_t a0, a1, a2;
+  if ((h & 1) == 0) {
+    a0 = w[0] >> 11;
+    a1 = w[1] >> 11;
+    a2 = w[2] >> 11;
+  } else {
+    a0 = w[3] >> 11;
+    a1 = ((w[0] & 0x7FFu) << 10) | (w[1] & 0x3FFu);
+    a2 = ((w[2] & 0x7FFu) << 10) | (w[3] & 0x3FFu);
+  }
+  const double sc = 1.0 / 2097152.0;
+  u[0] = a0 * sc;
+  u[1] = a1 * sc;
+  u[2] = a2 * sc;
+}
 
 /* ------------------------------------------------------------------------ */
 /* Pair, surface and field energies (FP64).                                  */
@@ -264,7 +297,6 @@ long orc_pass(const orc_params *p, float *ni, const int *pt, const float *ns, fl
               orc_trace *tr) {
   long acc = 0;
   long fed = 0;
-  uint32_t key[2] = {seed, stream};
   /* Sites of one pass are independent (no two are neighbours), so the
    * ORC_F_PARALLEL split over planes gives the same result as the serial
    * loop; fed uniforms are consumed in order and force the serial loop. */
@@ -283,11 +315,11 @@ long orc_pass(const orc_params *p, float *ni, const int *pt, const float *ns, fl
           u2 = feed[3 * fed + 2];
           fed++;
         } else {
-          uint32_t ctr[4] = {(uint32_t)s, (uint32_t)sweep, (uint32_t)(sweep >> 32), ORC_TAG_PLAIN}, r[4];
-          orc_philox(ctr, key, r);
-          u0 = u24(r[0]);
-          u1 = u24(r[1]);
-          u2 = u24(r[2]);
+          double u[3];
+          orc_site_uniforms(p->nx, p->ny, s, seed, stream, sweep, ORC_TAG_PLAIN, u);
+          u0 = u[0];
+          u1 = u[1];
+          u2 = u[2];
         }
         float cur[3] = {ni[3 * s], ni[3 * s + 1], ni[3 * s + 2]};
         double nold[3] = {cur[0], cur[1], cur[2]}, nnew[3];

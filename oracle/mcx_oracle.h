@@ -26,7 +26,7 @@ enum {
 };
 enum { ORC_ORDER_REDBLACK = 0, ORC_ORDER_EIGHT = 1 };
 enum { ORC_F_NO_NORMALIZE = 1, ORC_F_PARALLEL = 2 };
-enum { ORC_TAG_PLAIN = 0 };
+enum { ORC_TAG_PLAIN = 0, ORC_TAG_VMF = 2 };
 #define ORC_MAX_SURF 16
 
 typedef struct {
@@ -51,6 +51,8 @@ typedef struct {
 } orc_trace;
 
 void orc_philox(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
+void orc_site_uniforms(int nx, int ny, long s, uint32_t seed, uint32_t stream, uint64_t sweep, uint32_t tag,
+                       double u[3]);
 double orc_pair(const orc_params *p, const double ni[3], const double nj[3], int d, double *abs_out);
 double orc_surface(const orc_params *p, int sid, const double n[3], const double s[3], double *abs_out);
 double orc_field(const orc_params *p, const double n[3]);

@@ -172,6 +172,7 @@ def lib():
         L = C.CDLL(LIB_PATH)
         P, D, F, I, V = C.POINTER(_Params), C.c_double, C.c_float, C.c_int, C.c_void_p
         L.orc_philox.argtypes = [V, V, V]
+        L.orc_site_uniforms.argtypes = [I, I, C.c_long, C.c_uint32, C.c_uint32, C.c_uint64, C.c_uint32, V]
         L.orc_pair.argtypes = [P, V, V, I, V]
         L.orc_pair.restype = D
         L.orc_surface.argtypes = [P, I, V, V, V]
@@ -303,9 +304,18 @@ def propose(n, u0: float, u1: float, ang_var: float, flags: int = 0) -> np.ndarr
     return out
 
 
-def site_uniforms(site: int, seed: int, stream: int, sweep: int, tag: int = 0) -> np.ndarray:
-    r = philox([site, sweep & 0xFFFFFFFF, sweep >> 32, tag], [seed, stream])
-    return u24(r[:3])
+def site_uniforms(model_or_nx, ny_or_site, *args, tag: int = 0) -> np.ndarray:
+    """The (u0, u1, u2) a site update draws: site_uniforms(model, site, seed,
+    stream, sweep) or site_uniforms(nx, ny, site, seed, stream, sweep)."""
+    if isinstance(model_or_nx, Model):
+        nx, ny, site = model_or_nx.nx, model_or_nx.ny, ny_or_site
+        seed, stream, sweep = args
+    else:
+        nx, ny = model_or_nx, ny_or_site
+        site, seed, stream, sweep = args
+    u = np.zeros(3)
+    lib().orc_site_uniforms(nx, ny, int(site), seed, stream, sweep, tag, _ptr(u))
+    return u
 
 
 def adapt(ang_var: float, acc: int, valid: int) -> float:
@@ -350,6 +360,5 @@ def sweep_uniforms(model: Model, pt: np.ndarray, seed: int, stream: int, sweep: 
             m = ((i + j + k) & 1) == q
         m &= pt[s] != 0
         for site in s[m]:
-            r = philox([site, sweep & 0xFFFFFFFF, sweep >> 32, tag], [seed, stream])
-            out.append(u24(r[:3]))
+            out.append(site_uniforms(nx, ny, int(site), seed, stream, sweep, tag=tag))
     return np.array(out, dtype=np.float64).reshape(-1)

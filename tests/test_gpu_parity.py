@@ -79,7 +79,7 @@ def _check_pass(m, lat, before, dE_g, acc_g, prop_g, after, T, ang, seed, stream
     lat.ni[:] = before
     ties = 0
     for s in np.nonzero(upd)[0]:
-        u = O.site_uniforms(int(s), seed, stream, sweep)
+        u = O.site_uniforms(m, int(s), seed, stream, sweep)
         p64 = O.propose(before[s], u[0], u[1], ang)
         assert np.max(np.abs(prop_g[s] - p64)) < 3e-6, (s, prop_g[s], p64)
         e_new, a_new = lat.local_energy_abs(int(s), prop_g[s])
