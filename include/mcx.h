@@ -198,6 +198,15 @@ mcx_status mcx_debug_pass(mcx_engine *eng, int replica, int colour, float *dE, u
  * epilogue kernels; graph launches count each kernel node). */
 long long mcx_kernel_launches(const mcx_engine *eng);
 
+/* Chooses the sweep kernel: on != 0 the staged pass (tiles of rows brought
+ * into shared memory by TMA bulk copies, double-buffered, persistent CTAs),
+ * 0 the direct pass (each thread loads its neighbours from global memory).
+ * The direct pass is the default (it measures faster on the lattices
+ * benchmarked so far); the staged pass needs every replica's tile to fit in
+ * shared memory.  Both give bit-identical results. */
+mcx_status mcx_set_staged(mcx_engine *eng, int on);
+int mcx_get_staged(const mcx_engine *eng);
+
 /* The engine's CUDA stream (a cudaStream_t), for callers that record events
  * or order their own work against the engine's. */
 void *mcx_stream(mcx_engine *eng);

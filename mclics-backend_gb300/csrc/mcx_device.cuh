@@ -46,9 +46,15 @@ struct RepDev {
   int hp;     // same-colour site pairs per row, (hx + 1) / 2
   int npair;  // pairs per colour, hp*ny*nz: one thread each
   int plane;  // elements per (colour, component) plane, hs*ny*nz
-  int ncta;   // CTAs of this replica in one pass launch
+  int hps;    // point-type row stride in bytes (a multiple of 16)
+  int pplane; // point-type bytes per colour, hps*ny*nz
+  int ncta;   // CTAs of this replica in one direct pass launch
   uint32_t hp_m, ny_m;  // n / hp == (n * hp_m) >> hp_p for n < 2^31
   int hp_p, ny_p;
+  // tiles of the staged pass: tj x tk rows (tj | ny, tk | nz), ntile per colour
+  int tj, tk, ntj, ntile, tile0;  // tile0: index of the replica's first tile
+  uint32_t tj_m, ntj_m;
+  int tj_p, ntj_p;
   long long dir_off;  // float offset of this replica's [2][3][plane] block
   long long pt_off;   // byte offset of its [2][plane] point types
   long long ns_off;   // float offset of its [2][3][plane] normals

@@ -4,6 +4,7 @@
 // CUDA graphs of kChunk sweeps and replayed.
 #include <cuda_runtime.h>
 #include <stdarg.h>
+#include <stdlib.h>
 #include <stdio.h>
 #include <string.h>
 
@@ -53,6 +54,14 @@ struct mcx_engine {
   cudaGraphExec_t graph[2] = {nullptr, nullptr};  // [measure]
   long long launches = 0;
   std::string err;
+  // staged (TMA) pass
+  bool staged = false;      // sweeps use k_tpass
+  bool can_stage = false;   // every replica fits a stage
+  std::vector<int4> tiles;  // (replica, j0, k0, 0)
+  int4 *d_tiles = nullptr;
+  int stage_bytes = 0;
+  int grid[2] = {0, 0};     // persistent CTAs for [measure]
+  unsigned *d_err = nullptr;
 };
 
 static mcx_status fail(mcx_engine *e, mcx_status st, const char *fmt, ...) {
@@ -89,6 +98,46 @@ static void div_magic(uint32_t d, uint32_t &m, int &p) {
   m = (uint32_t)(((1ull << p) + d - 1) / d);
 }
 
+// Shared-memory bytes of one stage of the staged pass for a tj x tk tile.
+static long long stage_bytes_for(const RepDev &R, int tj, int tk, bool mask) {
+  const long long SA = (long long)tj * tk, SO = (long long)(tk + 2) * (tj + 2);
+  long long b = 12LL * R.hs * (SA + SO);
+  if (mask) b += (long long)R.hps * (SA + SO);
+  return align_up(b, 128);
+}
+
+// Chooses the staged pass's tile (tj | ny, tk | nz): as many site pairs as a
+// CTA's 256 threads can take twice over, weighted by the fraction of the
+// stage that is the tile itself rather than its halo, within the budget.
+static bool plan_tiles(RepDev &R, bool mask, long long budget) {
+  double best = -1;
+  int btj = 0, btk = 0;
+  for (int tk = 1; tk <= R.nz; tk++) {
+    if (R.nz % tk) continue;
+    for (int tj = 1; tj <= R.ny; tj++) {
+      if (R.ny % tj) continue;
+      const long long pairs = (long long)tj * tk * R.hp;
+      if (pairs > 1024) continue;
+      if (stage_bytes_for(R, tj, tk, mask) > budget) continue;
+      const double SA = (double)tj * tk, SO = (double)(tk + 2) * (tj + 2);
+      const double score = (double)std::min<long long>(pairs, 2 * kBlock) * SA / (SA + SO);
+      if (score > best) {
+        best = score;
+        btj = tj;
+        btk = tk;
+      }
+    }
+  }
+  if (btj == 0) return false;
+  R.tj = btj;
+  R.tk = btk;
+  R.ntj = R.ny / btj;
+  R.ntile = R.ntj * (R.nz / btk);
+  div_magic((uint32_t)btj, R.tj_m, R.tj_p);
+  div_magic((uint32_t)R.ntj, R.ntj_m, R.ntj_p);
+  return true;
+}
+
 extern "C" int mcx_version(void) { return 1; }
 
 extern "C" const char *mcx_last_error(const mcx_engine *e) { return e ? e->err.c_str() : g_last_error.c_str(); }
@@ -113,6 +162,8 @@ static void free_engine(mcx_engine *e) {
   cudaFree(e->d_mout);
   cudaFree(e->d_stage);
   cudaFree(e->d_stage_pt);
+  cudaFree(e->d_tiles);
+  cudaFree(e->d_err);
   if (e->stream) cudaStreamDestroy(e->stream);
   delete e;
 }
@@ -184,8 +235,10 @@ extern "C" mcx_status mcx_create(int n, const mcx_replica_desc *descs, mcx_engin
     div_magic((uint32_t)d.ny, R.ny_m, R.ny_p);
     R.dir_off = dir_total;
     dir_total += align_up(6LL * R.plane, 64);
+    R.hps = (int)align_up(R.hs, 16);
+    R.pplane = R.hps * d.ny * d.nz;
     R.pt_off = pt_total;
-    pt_total += align_up(2LL * R.plane, 256);
+    pt_total += align_up(2LL * R.pplane, 256);
     R.A = d.A;
     R.elecA = d.elecA;
     R.elecE = d.elecE;
@@ -220,6 +273,26 @@ extern "C" mcx_status mcx_create(int n, const mcx_replica_desc *descs, mcx_engin
     }
   }
   for (int r = 0; r < n; r++) e->rep[r].ns_off = e->var.mask ? e->rep[r].dir_off : -1;
+  {
+    const char *kb = getenv("MCX_STAGE_KB");
+    const long long budget = (kb ? atoll(kb) : 40) * 1024;
+    e->can_stage = true;
+    for (int r = 0; r < n && e->can_stage; r++) {
+      RepDev &R = e->rep[r];
+      if (!plan_tiles(R, e->var.mask, budget)) {
+        e->can_stage = false;
+        break;
+      }
+      R.tile0 = (int)e->tiles.size();
+      for (int kb2 = 0; kb2 < R.nz / R.tk; kb2++)
+        for (int jb = 0; jb < R.ntj; jb++) e->tiles.push_back(make_int4(r, jb * R.tj, kb2 * R.tk, 0));
+      e->stage_bytes = (int)std::max<long long>(e->stage_bytes, stage_bytes_for(R, R.tj, R.tk, e->var.mask));
+    }
+    // the direct pass measures faster on every lattice tried so far; the
+    // staged pass is opt-in (mcx_set_staged or MCX_STAGED=1)
+    const char *st = getenv("MCX_STAGED");
+    e->staged = e->can_stage && st && atoi(st) == 1;
+  }
   mcx_status st = MCX_OK;
 #define CKC(call)                                                                                  \
   do {                                                                                             \
@@ -249,6 +322,22 @@ extern "C" mcx_status mcx_create(int n, const mcx_replica_desc *descs, mcx_engin
   CKC(cudaMalloc(&e->d_stats, sizeof(double) * kStats * n));
   CKC(cudaMemsetAsync(e->d_stats, 0, sizeof(double) * kStats * n, e->stream));
   CKC(cudaMalloc(&e->d_mout, sizeof(double) * 16 * n));
+  CKC(cudaMalloc(&e->d_err, sizeof(unsigned)));
+  CKC(cudaMemsetAsync(e->d_err, 0, sizeof(unsigned), e->stream));
+  if (e->can_stage) {
+    CKC(cudaMalloc(&e->d_tiles, sizeof(int4) * e->tiles.size()));
+    CKC(cudaMemcpyAsync(e->d_tiles, e->tiles.data(), sizeof(int4) * e->tiles.size(), cudaMemcpyHostToDevice, e->stream));
+    int dev = 0, nsm = 0;
+    CKC(cudaGetDevice(&dev));
+    CKC(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    for (int m = 0; m < 2; m++) {
+      const int per = tpass_blocks_per_sm(e->var, m ? MODE_SWEEP_MEASURE : MODE_SWEEP, e->stage_bytes);
+      e->grid[m] = std::min<long long>((long long)per * nsm, (long long)e->tiles.size());
+      if (per <= 0) e->can_stage = e->staged = false;
+    }
+    // the trace specialisation (parity checks) needs the same shared-memory opt-in
+    if (e->can_stage && tpass_blocks_per_sm(e->var, MODE_TRACE, e->stage_bytes) <= 0) e->can_stage = e->staged = false;
+  }
   CKC(cudaMalloc(&e->d_stage, sizeof(float) * 3 * e->max_sites));
   CKC(cudaMalloc(&e->d_stage_pt, sizeof(int) * e->max_sites));
   CKC(cudaMemcpyAsync(e->d_map, e->map.data(), sizeof(int2) * e->map.size(), cudaMemcpyHostToDevice, e->stream));
@@ -447,17 +536,25 @@ static PassArgs pass_args(mcx_engine *e) {
   pa.stats = e->d_stats;
   pa.ring = e->d_ring;
   pa.ring_cap = e->ring_cap;
+  pa.tiles = e->d_tiles;
+  pa.ntiles = (int)e->tiles.size();
+  pa.stage_bytes = e->stage_bytes;
+  pa.err = e->d_err;
   return pa;
+}
+
+// One red/black pass of every replica, staged or direct.
+static void launch_sweep_pass(mcx_engine *e, PassArgs &pa, int colour, bool measure) {
+  pa.colour = colour;
+  const int mode = measure ? MODE_SWEEP_MEASURE : MODE_SWEEP;
+  if (e->staged) launch_tpass(e->var, mode, pa, e->grid[measure ? 1 : 0], e->stream);
+  else launch_pass(e->var, mode, pa, (int)e->map.size(), e->stream);
 }
 
 // One sweep's kernels on e->stream: the two colours.
 static void enqueue_sweep(mcx_engine *e, bool measure) {
   PassArgs pa = pass_args(e);
-  const int nb = (int)e->map.size();
-  for (int c = 0; c < 2; c++) {
-    pa.colour = c;
-    launch_pass(e->var, measure ? MODE_SWEEP_MEASURE : MODE_SWEEP, pa, nb, e->stream);
-  }
+  for (int c = 0; c < 2; c++) launch_sweep_pass(e, pa, c, measure);
 }
 
 static mcx_status build_graph(mcx_engine *e, int measure) {
@@ -519,11 +616,37 @@ extern "C" mcx_status mcx_sweep(mcx_engine *e, int n, int measure) {
   return MCX_OK;
 }
 
+// Reads (and clears) the staged pass's timeout flag after a synchronisation.
+static mcx_status check_err_flag(mcx_engine *e) {
+  unsigned f = 0;
+  CK(e, cudaMemcpy(&f, e->d_err, sizeof f, cudaMemcpyDeviceToHost));
+  if (f) {
+    CK(e, cudaMemset(e->d_err, 0, sizeof f));
+    return fail(e, MCX_ERR_CUDA, "staged pass: a shared-memory tile copy did not complete in time; results are invalid");
+  }
+  return MCX_OK;
+}
+
 extern "C" mcx_status mcx_sync(mcx_engine *e) {
   if (!e) return fail(nullptr, MCX_ERR_INVALID, "null engine");
   CK(e, cudaStreamSynchronize(e->stream));
+  return check_err_flag(e);
+}
+
+extern "C" mcx_status mcx_set_staged(mcx_engine *e, int on) {
+  if (!e) return fail(nullptr, MCX_ERR_INVALID, "null engine");
+  if (on && !e->can_stage) return fail(e, MCX_ERR_UNSUPPORTED, "a replica's rows do not fit the staged pass's shared memory");
+  CK(e, cudaStreamSynchronize(e->stream));
+  e->staged = on != 0;
+  for (int m = 0; m < 2; m++)
+    if (e->graph[m]) {
+      cudaGraphExecDestroy(e->graph[m]);
+      e->graph[m] = nullptr;
+    }
   return MCX_OK;
 }
+
+extern "C" int mcx_get_staged(const mcx_engine *e) { return e && e->staged ? 1 : 0; }
 
 extern "C" mcx_status mcx_measure(mcx_engine *e, int r, double *out) {
   if (mcx_status st = check_rep(e, r)) return st;
@@ -548,7 +671,7 @@ extern "C" mcx_status mcx_get_stats(mcx_engine *e, int r, double *out) {
   CK(e, cudaMemcpyAsync(out, e->d_stats + (size_t)r * kStats, sizeof(double) * kStats, cudaMemcpyDeviceToHost,
                         e->stream));
   CK(e, cudaStreamSynchronize(e->stream));
-  return MCX_OK;
+  return check_err_flag(e);
 }
 
 extern "C" mcx_status mcx_reset_stats(mcx_engine *e, int r) {
@@ -607,12 +730,10 @@ extern "C" mcx_status mcx_pass_timing(mcx_engine *e, int n, float *pass_ms, floa
   std::vector<cudaEvent_t> ev(4 * (size_t)n);
   for (auto &x : ev) CK(e, cudaEventCreate(&x));
   PassArgs pa = pass_args(e);
-  const int nb = (int)e->map.size();
   for (int s = 0; s < n; s++)
     for (int c = 0; c < 2; c++) {
-      pa.colour = c;
       CK(e, cudaEventRecord(ev[4 * s + 2 * c], e->stream));
-      launch_pass(e->var, MODE_SWEEP, pa, nb, e->stream);
+      launch_sweep_pass(e, pa, c, false);
       CK(e, cudaEventRecord(ev[4 * s + 2 * c + 1], e->stream));
     }
   e->launches += 2LL * n;
@@ -683,7 +804,18 @@ extern "C" mcx_status mcx_debug_pass(mcx_engine *e, int r, int colour, float *dE
   pa.tr_dE = d_dE;
   pa.tr_acc = d_acc;
   pa.tr_prop = d_prop;
-  launch_pass(e->var, MODE_TRACE, pa, (int)sub.size(), e->stream);
+  int4 *d_sub_tiles = nullptr;
+  if (e->staged) {
+    const RepDev &Rr = e->rep[r];
+    CK(e, cudaMalloc(&d_sub_tiles, sizeof(int4) * Rr.ntile));
+    CK(e, cudaMemcpyAsync(d_sub_tiles, e->tiles.data() + Rr.tile0, sizeof(int4) * Rr.ntile, cudaMemcpyHostToDevice,
+                          e->stream));
+    pa.tiles = d_sub_tiles;
+    pa.ntiles = Rr.ntile;
+    launch_tpass(e->var, MODE_TRACE, pa, std::min(e->grid[0], Rr.ntile), e->stream);
+  } else {
+    launch_pass(e->var, MODE_TRACE, pa, (int)sub.size(), e->stream);
+  }
   e->launches += 1;
   CKL(e);
   if (dE) CK(e, cudaMemcpyAsync(dE, d_dE, sizeof(float) * R.ntot, cudaMemcpyDeviceToHost, e->stream));
@@ -694,5 +826,6 @@ extern "C" mcx_status mcx_debug_pass(mcx_engine *e, int r, int colour, float *dE
   cudaFree(d_prop);
   cudaFree(d_acc);
   cudaFree(d_map);
-  return MCX_OK;
+  cudaFree(d_sub_tiles);
+  return check_err_flag(e);
 }

@@ -211,8 +211,9 @@ __global__ void __launch_bounds__(kBlock, MCX_PASS_MIN_BLOCKS) k_pass(PassArgs a
     const int off = row * hs + h0;
     float *Ac = a.dir + R.dir_off + (long long)(c * 3) * P;
     const float *Oc = a.dir + R.dir_off + (long long)((c ^ 1) * 3) * P;
-    const uint8_t *pa = a.pt + R.pt_off + (long long)c * P;
-    const uint8_t *po = a.pt + R.pt_off + (long long)(c ^ 1) * P;
+    const uint8_t *pa = a.pt + R.pt_off + (long long)c * R.pplane;
+    const uint8_t *po = a.pt + R.pt_off + (long long)(c ^ 1) * R.pplane;
+    const int offp = row * R.hps + h0;
     // own pair and the other colour's pair at the same position
     float2 ax = *reinterpret_cast<const float2 *>(Ac + off);
     float2 ay = *reinterpret_cast<const float2 *>(Ac + off + P);
@@ -249,14 +250,14 @@ __global__ void __launch_bounds__(kBlock, MCX_PASS_MIN_BLOCKS) k_pass(PassArgs a
       nr[d][0] = __ldg(reinterpret_cast<const float2 *>(Oc + ro));
       nr[d][1] = __ldg(reinterpret_cast<const float2 *>(Oc + ro + P));
       nr[d][2] = __ldg(reinterpret_cast<const float2 *>(Oc + ro + 2 * P));
-      if (MASK) pr[d] = __ldg(reinterpret_cast<const uchar2 *>(po + ro));
+      if (MASK) pr[d] = __ldg(reinterpret_cast<const uchar2 *>(po + (er[d] != 0.f ? rr[d] * R.hps + h0 : offp)));
     }
     uchar2 pself2 = make_uchar2(1, 1), po2 = make_uchar2(1, 1);
     uint8_t pex = 1;
     if (MASK) {
-      pself2 = __ldg(reinterpret_cast<const uchar2 *>(pa + off));
-      po2 = __ldg(reinterpret_cast<const uchar2 *>(po + off));
-      pex = __ldg(po + exo);
+      pself2 = __ldg(reinterpret_cast<const uchar2 *>(pa + offp));
+      po2 = __ldg(reinterpret_cast<const uchar2 *>(po + offp));
+      pex = __ldg(po + (exe != 0.f ? row * R.hps + exh : offp));
     }
     float uA[3] = {0.f, 0.f, 0.f}, uB[3] = {0.f, 0.f, 0.f};
     float ang = 0.f, invT = 0.f;
@@ -404,6 +405,461 @@ __global__ void __launch_bounds__(kBlock, MCX_PASS_MIN_BLOCKS) k_pass(PassArgs a
       st[12] = (double)S->sweep;
     }
   }
+}
+
+// ---------------------------------------------------------------------------
+// Staged pass: tiles of rows brought into shared memory by TMA bulk copies.
+//
+// A tile is tj x tk rows (tj | ny, tk | nz) of one replica.  For colour c it
+// needs the tile's own rows (A) and the other colour's rows with a one-row
+// halo in j and k (O): every row is a contiguous hs-float run in the split
+// layout, so each is one cp.async.bulk (rows of a plane merge into one copy).
+// Stage layout: A [3][tj*tk][hs] floats, O [3][(tk+2)*(tj+2)][hs] floats,
+// then the point types Ap [tj*tk][hps], Op [(tk+2)*(tj+2)][hps] bytes.  O slot
+// of row (jl, kl) relative to the tile is (kl+1)*(tj+2) + jl+1; corner slots
+// are never filled or read.  Absent rows (free boundaries) are not copied and
+// are read with weight 0 (shared memory is zeroed once, so stale values are
+// finite).  Each persistent CTA double-buffers: the next tile's copies fly
+// while the current tile is updated; completion is tracked by one mbarrier
+// per stage (arrive.expect_tx + complete_tx), and every wait is bounded.
+// ---------------------------------------------------------------------------
+#ifndef MCX_TPASS_MIN_BLOCKS
+#define MCX_TPASS_MIN_BLOCKS 3
+#endif
+#ifndef MCX_TPASS_STAGES
+#define MCX_TPASS_STAGES 3
+#endif
+constexpr int kStages = MCX_TPASS_STAGES;
+constexpr long long kWaitLimit = 1LL << 26;  // try_wait polls before giving up
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait for a stage's copies; false when the limit ran out.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
+  for (long long i = 0; i < kWaitLimit; i++)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+
+__device__ __forceinline__ void bulk_copy_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+struct StageView {
+  float *A, *O;
+  uint8_t *Ap, *Op;
+  int SA, SO;
+};
+
+__device__ __forceinline__ StageView stage_view(char *base, const RepDev &R) {
+  StageView v;
+  v.SA = R.tj * R.tk;
+  v.SO = (R.tk + 2) * (R.tj + 2);
+  v.A = reinterpret_cast<float *>(base);
+  v.O = v.A + 3 * v.SA * R.hs;
+  v.Ap = reinterpret_cast<uint8_t *>(v.O + 3 * v.SO * R.hs);
+  v.Op = v.Ap + v.SA * R.hps;
+  return v;
+}
+
+// Copy i of a tile (i < (4 tk + 2) * (3 + MASK)): component q = i / nseg
+// (q = 3: point types), segment g = i % nseg.  Segments 0 .. tk-1 are the
+// tile's own rows of plane k0 + g; then the other colour's planes k0-1 (one
+// run), k0 .. k0+tk-1 (three runs each: the tj tile rows, the row below, the
+// row above) and k0+tk (one run).  Returns the byte count, 0 when the rows
+// are absent (free boundary).
+template <bool MASK>
+__device__ __forceinline__ uint32_t tile_copy(const PassArgs &a, const RepDev &R, int c, int j0, int k0,
+                                              const StageView &v, int i, void *&dst, const void *&src) {
+  const int hs = R.hs, tj = R.tj, tk = R.tk, ny = R.ny, nz = R.nz, P = R.plane, hps = R.hps;
+  const int nseg = 4 * tk + 2;
+  const int q = i / nseg, g = i - q * nseg;
+  const bool ptq = MASK && q == 3;
+  if (g < tk) {
+    const int row = j0 + ny * (k0 + g);
+    if (ptq) {
+      dst = v.Ap + (size_t)g * tj * hps;
+      src = a.pt + R.pt_off + (long long)c * R.pplane + (long long)row * hps;
+      return (uint32_t)(tj * hps);
+    }
+    dst = v.A + ((size_t)q * v.SA + g * tj) * hs;
+    src = a.dir + R.dir_off + (long long)(c * 3 + q) * P + (long long)row * hs;
+    return (uint32_t)(tj * hs * 4);
+  }
+  const int o = g - tk;
+  int kl, jl, nrows;
+  if (o == 0) {
+    kl = -1; jl = 0; nrows = tj;
+  } else if (o == 3 * tk + 1) {
+    kl = tk; jl = 0; nrows = tj;
+  } else {
+    kl = (o - 1) / 3;
+    const int run = (o - 1) - 3 * kl;
+    jl = run == 0 ? 0 : (run == 1 ? -1 : tj);
+    nrows = run == 0 ? tj : 1;
+  }
+  int k = k0 + kl;
+  if (k < 0 || k >= nz) {
+    if (R.zb != BOUND_PERIODIC) return 0;
+    k = (k + nz) % nz;
+  }
+  int j = j0 + jl;
+  if (j < 0 || j >= ny) {
+    if (R.yb != BOUND_PERIODIC) return 0;
+    j = (j + ny) % ny;
+  }
+  const int slot = (kl + 1) * (tj + 2) + jl + 1;
+  const int row = j + ny * k;
+  if (ptq) {
+    dst = v.Op + (size_t)slot * hps;
+    src = a.pt + R.pt_off + (long long)(c ^ 1) * R.pplane + (long long)row * hps;
+    return (uint32_t)(nrows * hps);
+  }
+  dst = v.O + ((size_t)q * v.SO + slot) * hs;
+  src = a.dir + R.dir_off + (long long)((c ^ 1) * 3 + q) * P + (long long)row * hs;
+  return (uint32_t)(nrows * hs * 4);
+}
+
+// Issued by the 32 lanes of warp 0 together: the byte total is warp-reduced
+// and registered on the stage's mbarrier by lane 0 before any copy starts.
+template <bool MASK>
+__device__ __forceinline__ void issue_tile(const PassArgs &a, int c, int t, char *stage, uint64_t *bar) {
+  const int4 td = a.tiles[t];
+  const RepDev &R = a.reps[td.x];
+  const StageView v = stage_view(stage, R);
+  const int lane = threadIdx.x & 31;
+  const int ncopy = (4 * R.tk + 2) * (MASK ? 4 : 3);
+  uint32_t bytes = 0;
+  for (int i = lane; i < ncopy; i += 32) {
+    void *d;
+    const void *sp;
+    bytes += tile_copy<MASK>(a, R, c, td.y, td.z, v, i, d, sp);
+  }
+  bytes = __reduce_add_sync(0xffffffffu, bytes);
+  if (lane == 0) mbar_arrive_expect_tx(bar, bytes);
+  __syncwarp();
+  for (int i = lane; i < ncopy; i += 32) {
+    void *d;
+    const void *sp;
+    const uint32_t b = tile_copy<MASK>(a, R, c, td.y, td.z, v, i, d, sp);
+    if (b) bulk_copy_g2s(d, sp, b, bar);
+  }
+}
+
+// Block-wide: adds this CTA's acceptance and measurement sums for replica r,
+// counts `tiles` finished tiles, and lets the CTA that finishes the
+// replica's last tile of a colour-1 sweep pass apply the step-size rule.
+template <int MODE>
+__device__ __forceinline__ void flush_replica(const PassArgs &a, int r, int tiles, unsigned acc, float qs[kQ],
+                                              bool mask) {
+  constexpr bool MEAS = MODE == MODE_SWEEP_MEASURE;
+  constexpr bool TRACE = MODE == MODE_TRACE;
+  __shared__ unsigned s_acc[kBlock / 32];
+  __shared__ float s_q[kBlock / 32][kQ];
+  __shared__ unsigned s_last;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const RepDev &R = a.reps[r];
+  RepState *S = a.st + r;
+  if (!TRACE) {
+    const unsigned wa = __reduce_add_sync(0xffffffffu, acc);
+    if (lane == 0) s_acc[wid] = wa;
+  }
+  if (MEAS) {
+#pragma unroll
+    for (int q = 0; q < kQ; q++) {
+      float v = qs[q];
+#pragma unroll
+      for (int o2 = 16; o2 > 0; o2 >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o2);
+      if (lane == 0) s_q[wid][q] = v;
+    }
+  }
+  __syncthreads();
+  const int lane_slot = blockIdx.x % kLanes;
+  if (!TRACE && threadIdx.x == 0) {
+    unsigned tot = 0;
+#pragma unroll
+    for (int w2 = 0; w2 < kBlock / 32; w2++) tot += s_acc[w2];
+    if (tot) atomicAdd(&S->acc[lane_slot], tot);
+    __threadfence();
+  }
+  if (MEAS && threadIdx.x < kQ) {
+    const int q = (!mask && threadIdx.x == 1) ? 0 : threadIdx.x;
+    float v = 0.f;
+#pragma unroll
+    for (int w2 = 0; w2 < kBlock / 32; w2++) v += s_q[w2][q];
+    const unsigned long long slot = S->meas % (unsigned long long)a.ring_cap;
+    double *ring = a.ring + (((size_t)r * (a.ring_cap + 1) + slot) * kLanes + lane_slot) * kQ;
+    atomicAdd(ring + threadIdx.x, (double)v);
+    __threadfence();
+  }
+  if (!TRACE && a.colour == 1) {
+    __syncthreads();
+    if (threadIdx.x == 0) s_last = atomicAdd(&S->done, (unsigned)tiles) + (unsigned)tiles == (unsigned)R.ntile;
+    __syncthreads();
+    if (s_last && threadIdx.x == 0) {
+      __threadfence();
+      unsigned tot = 0;
+#pragma unroll
+      for (int l = 0; l < kLanes; l++) tot += atomicExch(&S->acc[l], 0u);
+      // src/evolve.cpp:169-178 with the reference's float/double rounding
+      float av = S->ang_var;
+      const double ratio = 1.0 * (double)tot / (double)R.valid;
+      if (ratio < 0.5) {
+        av = (float)((double)av * 0.99);
+        if ((double)av < 0.01) av = (float)0.01;
+      } else if (ratio > 0.5) {
+        av = (float)((double)av / 0.99);
+        if ((double)av > 1.0) av = (float)((double)av - 0.5);
+      }
+      S->ang_var = av;
+      S->sweep += 1;
+      if (MEAS) S->meas += 1;
+      S->done = 0;
+      double *st = a.stats + (size_t)r * kStats;
+      st[7] += (double)tot;
+      st[8] += 1.0;
+      st[11] = (double)av;
+      st[12] = (double)S->sweep;
+    }
+  }
+  __syncthreads();
+}
+
+template <int POT, bool MASK, bool FIELD, int MODE>
+__device__ __forceinline__ void compute_tile(const PassArgs &a, const RepDev &R, RepState *S, int c, int j0, int k0,
+                                             const StageView &v, unsigned &acc, float qs[kQ]) {
+  constexpr bool UPD = MODE != MODE_MEASURE_ONLY;
+  const int hx = R.hx, ny = R.ny, nz = R.nz, hs = R.hs, hps = R.hps, tj = R.tj, P = R.plane;
+  const int SA = v.SA, SO = v.SO, tjs = tj + 2;
+  const int npairs = tj * R.tk * R.hp;
+  float *gA = a.dir + R.dir_off + (long long)(c * 3) * P;
+  const unsigned long long sw = S->sweep;
+  const float ang = S->ang_var;
+  const float invT = 1.0f / S->T;
+  for (int p = threadIdx.x; p < npairs; p += kBlock) {
+    const int rl = (int)fastdiv((uint32_t)p, R.hp_m, R.hp_p);
+    const int h0 = 2 * (p - rl * R.hp);
+    const int kl = (int)fastdiv((uint32_t)rl, R.tj_m, R.tj_p);
+    const int jl = rl - kl * tj;
+    const int j = j0 + jl, k = k0 + kl;
+    const int row = j + ny * k;
+    const int s = (c + j + k) & 1;
+    const bool hasB = h0 + 1 < hx;
+    const int aslot = kl * tj + jl;
+    const int oslot = (kl + 1) * tjs + jl + 1;
+    const float *As = v.A + (size_t)aslot * hs + h0;
+    const float *Os = v.O + (size_t)oslot * hs;
+    float2 ax = *reinterpret_cast<const float2 *>(As);
+    float2 ay = *reinterpret_cast<const float2 *>(As + (size_t)SA * hs);
+    float2 az = *reinterpret_cast<const float2 *>(As + (size_t)2 * SA * hs);
+    const float2 ox = *reinterpret_cast<const float2 *>(Os + h0);
+    const float2 oy = *reinterpret_cast<const float2 *>(Os + (size_t)SO * hs + h0);
+    const float2 oz = *reinterpret_cast<const float2 *>(Os + (size_t)2 * SO * hs + h0);
+    int exh;
+    float exe = 1.f;
+    if (s == 0) {
+      exh = h0 - 1;
+      if (exh < 0) { if (R.xb == BOUND_PERIODIC) exh = hx - 1; else { exe = 0.f; exh = h0; } }
+    } else {
+      exh = hasB ? h0 + 2 : h0 + 1;
+      if (exh == hx) { if (R.xb == BOUND_PERIODIC) exh = 0; else { exe = 0.f; exh = h0; } }
+    }
+    const float ex = Os[exh], ey = Os[(size_t)SO * hs + exh], ez = Os[(size_t)2 * SO * hs + exh];
+    float er[4] = {1.f, 1.f, 1.f, 1.f};
+    if (j + 1 == ny && R.yb != BOUND_PERIODIC) er[0] = 0.f;
+    if (j == 0 && R.yb != BOUND_PERIODIC) er[1] = 0.f;
+    if (k + 1 == nz && R.zb != BOUND_PERIODIC) er[2] = 0.f;
+    if (k == 0 && R.zb != BOUND_PERIODIC) er[3] = 0.f;
+    const int rslot[4] = {oslot + 1, oslot - 1, oslot + tjs, oslot - tjs};
+    float2 nr[4][3];
+    uchar2 pr[4];
+#pragma unroll
+    for (int d = 0; d < 4; d++) {
+      const float *Ro = v.O + (size_t)rslot[d] * hs + h0;
+      nr[d][0] = *reinterpret_cast<const float2 *>(Ro);
+      nr[d][1] = *reinterpret_cast<const float2 *>(Ro + (size_t)SO * hs);
+      nr[d][2] = *reinterpret_cast<const float2 *>(Ro + (size_t)2 * SO * hs);
+      if (MASK) pr[d] = *reinterpret_cast<const uchar2 *>(v.Op + (size_t)rslot[d] * hps + h0);
+    }
+    uchar2 pself2 = make_uchar2(1, 1), po2 = make_uchar2(1, 1);
+    uint8_t pex = 1;
+    if (MASK) {
+      pself2 = *reinterpret_cast<const uchar2 *>(v.Ap + (size_t)aslot * hps + h0);
+      po2 = *reinterpret_cast<const uchar2 *>(v.Op + (size_t)oslot * hps + h0);
+      pex = v.Op[(size_t)oslot * hps + exh];
+    }
+    float uA[3] = {0.f, 0.f, 0.f}, uB[3] = {0.f, 0.f, 0.f};
+    if (UPD) {
+      const uint32_t pid = (uint32_t)row * (uint32_t)R.hp + (uint32_t)(h0 >> 1);
+      const uint4 rw = philox4x32_10(make_uint4(pid, (uint32_t)sw, (uint32_t)(sw >> 32), TAG_PLAIN | (uint32_t)c),
+                                     R.seed, R.stream);
+      pair_uniforms(rw, uA, uB);
+    }
+    auto wt = [&](float ee, uint8_t pp) { return MASK ? (ee != 0.f && pp != 0 ? 1.f : 0.f) : ee; };
+    float nb[6][3], w[6], e[6];
+    {
+      if (s == 0) {
+        nb[0][0] = ox.x; nb[0][1] = oy.x; nb[0][2] = oz.x; e[0] = 1.f; w[0] = wt(1.f, po2.x);
+        nb[1][0] = ex; nb[1][1] = ey; nb[1][2] = ez; e[1] = exe; w[1] = wt(exe, pex);
+      } else {
+        if (hasB) {
+          nb[0][0] = ox.y; nb[0][1] = oy.y; nb[0][2] = oz.y; e[0] = 1.f; w[0] = wt(1.f, po2.y);
+        } else {
+          nb[0][0] = ex; nb[0][1] = ey; nb[0][2] = ez; e[0] = exe; w[0] = wt(exe, pex);
+        }
+        nb[1][0] = ox.x; nb[1][1] = oy.x; nb[1][2] = oz.x; e[1] = 1.f; w[1] = wt(1.f, po2.x);
+      }
+#pragma unroll
+      for (int d = 0; d < 4; d++) {
+        nb[2 + d][0] = nr[d][0].x; nb[2 + d][1] = nr[d][1].x; nb[2 + d][2] = nr[d][2].x;
+        e[2 + d] = er[d];
+        w[2 + d] = wt(er[d], MASK ? pr[d].x : 1);
+      }
+      const int ps = MASK ? pself2.x : 1;
+      float sx = 0.f, sy = 0.f, sz = 0.f;
+      if (MASK && ps > 1) {
+        const float *nsb = a.ns + R.ns_off + (long long)(c * 3) * P + (long long)row * hs + h0;
+        sx = __ldg(nsb);
+        sy = __ldg(nsb + P);
+        sz = __ldg(nsb + 2 * P);
+      }
+      const uint32_t nat = (uint32_t)(2 * h0 + s) + (uint32_t)R.nx * (uint32_t)row;
+      acc += site_update<POT, MASK, FIELD, MODE>(R, a, c, ax.x, ay.x, az.x, nb, w, e, ps, sx, sy, sz, uA, ang, invT,
+                                                 nat, qs);
+    }
+    if (hasB) {
+      if (s == 0) {
+        nb[0][0] = ox.y; nb[0][1] = oy.y; nb[0][2] = oz.y; e[0] = 1.f; w[0] = wt(1.f, po2.y);
+        nb[1][0] = ox.x; nb[1][1] = oy.x; nb[1][2] = oz.x; e[1] = 1.f; w[1] = wt(1.f, po2.x);
+      } else {
+        nb[0][0] = ex; nb[0][1] = ey; nb[0][2] = ez; e[0] = exe; w[0] = wt(exe, pex);
+        nb[1][0] = ox.y; nb[1][1] = oy.y; nb[1][2] = oz.y; e[1] = 1.f; w[1] = wt(1.f, po2.y);
+      }
+#pragma unroll
+      for (int d = 0; d < 4; d++) {
+        nb[2 + d][0] = nr[d][0].y; nb[2 + d][1] = nr[d][1].y; nb[2 + d][2] = nr[d][2].y;
+        e[2 + d] = er[d];
+        w[2 + d] = wt(er[d], MASK ? pr[d].y : 1);
+      }
+      const int ps = MASK ? pself2.y : 1;
+      float sx = 0.f, sy = 0.f, sz = 0.f;
+      if (MASK && ps > 1) {
+        const float *nsb = a.ns + R.ns_off + (long long)(c * 3) * P + (long long)row * hs + h0 + 1;
+        sx = __ldg(nsb);
+        sy = __ldg(nsb + P);
+        sz = __ldg(nsb + 2 * P);
+      }
+      const uint32_t nat = (uint32_t)(2 * h0 + 2 + s) + (uint32_t)R.nx * (uint32_t)row;
+      acc += site_update<POT, MASK, FIELD, MODE>(R, a, c, ax.y, ay.y, az.y, nb, w, e, ps, sx, sy, sz, uB, ang, invT,
+                                                 nat, qs);
+    }
+    if (UPD) {
+      float *g = gA + (long long)row * hs + h0;
+      *reinterpret_cast<float2 *>(g) = ax;
+      *reinterpret_cast<float2 *>(g + P) = ay;
+      *reinterpret_cast<float2 *>(g + 2 * P) = az;
+    }
+  }
+}
+
+template <int POT, bool MASK, bool FIELD, int MODE>
+__global__ void __launch_bounds__(kBlock, MCX_TPASS_MIN_BLOCKS) k_tpass(PassArgs a) {
+  extern __shared__ __align__(128) char smem[];
+  __shared__ __align__(8) uint64_t bars[kStages];
+  __shared__ int s_ok;
+  const int c = a.colour;
+  // zero the stages once: rows that are never copied (absent halos, corner
+  // slots) must hold finite values
+  for (int i = threadIdx.x; i < kStages * a.stage_bytes / 16; i += kBlock)
+    reinterpret_cast<float4 *>(smem)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (threadIdx.x == 0) {
+    for (int q = 0; q < kStages; q++) mbar_init(&bars[q], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  const int G = gridDim.x;
+  const bool producer = threadIdx.x < 32;
+  // prologue: the first kStages-1 tiles
+  if (producer) {
+    fence_proxy_async();
+    for (int q = 0; q < kStages - 1; q++) {
+      const int tq = blockIdx.x + q * G;
+      if (tq < a.ntiles) issue_tile<MASK>(a, c, tq, smem + q * a.stage_bytes, &bars[q]);
+    }
+  }
+  int cur = -1, ntl = 0;
+  unsigned acc = 0;
+  float qs[kQ];
+#pragma unroll
+  for (int q = 0; q < kQ; q++) qs[q] = 0.f;
+  int it = 0;
+  for (int t = blockIdx.x; t < a.ntiles; it++, t += G) {
+    const int sidx = it % kStages;
+    const int4 td = a.tiles[t];
+    if (td.x != cur) {
+      if (cur >= 0) {
+        flush_replica<MODE>(a, cur, ntl, acc, qs, MASK);
+        acc = 0;
+#pragma unroll
+        for (int q = 0; q < kQ; q++) qs[q] = 0.f;
+      }
+      cur = td.x;
+      ntl = 0;
+    }
+    if (producer) {
+      // refill the stage the previous iteration released
+      const int tn = t + (kStages - 1) * G;
+      if (tn < a.ntiles) {
+        const int sn = (it + kStages - 1) % kStages;
+        fence_proxy_async();
+        issue_tile<MASK>(a, c, tn, smem + sn * a.stage_bytes, &bars[sn]);
+      }
+      if (threadIdx.x == 0) s_ok = mbar_wait(&bars[sidx], (uint32_t)((it / kStages) & 1)) ? 1 : 0;
+    }
+    __syncthreads();
+    if (!s_ok) {
+      // a stage never completed: report it, let the copies still in flight
+      // land (bounded), and leave without touching the sums
+      if (threadIdx.x == 0) {
+        atomicExch(a.err, 1u);
+        for (int q = 0; q < kStages; q++) {
+          const int last = it + q;  // iterations whose copies may be in flight
+          const int tq = blockIdx.x + last * G;
+          if (tq < a.ntiles) mbar_wait(&bars[last % kStages], (uint32_t)((last / kStages) & 1));
+        }
+      }
+      return;
+    }
+    const RepDev &R = a.reps[td.x];
+    compute_tile<POT, MASK, FIELD, MODE>(a, R, a.st + td.x, c, td.y, td.z,
+                                         stage_view(smem + sidx * a.stage_bytes, R), acc, qs);
+    ntl++;
+    __syncthreads();
+  }
+  if (cur >= 0) flush_replica<MODE>(a, cur, ntl, acc, qs, MASK);
 }
 
 // ---------------------------------------------------------------------------
@@ -565,19 +1021,22 @@ __global__ void k_measure_out(const RepDev *reps, double *ring, int ring_cap, in
 // ---------------------------------------------------------------------------
 // Layout conversion and initial conditions (one replica, natural site order).
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ long long split_index(const RepDev &R, long long s, int &c) {
+__device__ __forceinline__ long long split_index(const RepDev &R, long long s, int &c, long long &row, int &h) {
   const int i = (int)(s % R.nx);
-  const long long t = s / R.nx;
-  const int j = (int)(t % R.ny), k = (int)(t / R.ny);
+  row = s / R.nx;
+  const int j = (int)(row % R.ny), k = (int)(row / R.ny);
   c = (i + j + k) & 1;
-  return ((long long)j + (long long)R.ny * k) * R.hs + (i >> 1);
+  h = i >> 1;
+  return row * R.hs + h;
 }
 
 __global__ void k_aos_to_split(RepDev R, const float *__restrict__ aos, float *__restrict__ dir) {
   const long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= R.ntot) return;
-  int c;
-  const long long p = split_index(R, s, c);
+  int c, h;
+  long long row;
+  const long long p = split_index(R, s, c, row, h);
+  const long long pp = row * R.hps + h;
   float *d = dir + R.dir_off + (long long)(c * 3) * R.plane + p;
   d[0] = aos[3 * s];
   d[R.plane] = aos[3 * s + 1];
@@ -587,8 +1046,10 @@ __global__ void k_aos_to_split(RepDev R, const float *__restrict__ aos, float *_
 __global__ void k_split_to_aos(RepDev R, const float *__restrict__ dir, float *__restrict__ aos) {
   const long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= R.ntot) return;
-  int c;
-  const long long p = split_index(R, s, c);
+  int c, h;
+  long long row;
+  const long long p = split_index(R, s, c, row, h);
+  const long long pp = row * R.hps + h;
   const float *d = dir + R.dir_off + (long long)(c * 3) * R.plane + p;
   aos[3 * s] = d[0];
   aos[3 * s + 1] = d[R.plane];
@@ -599,9 +1060,11 @@ __global__ void k_mask_to_split(RepDev R, const int *__restrict__ pt_aos, const 
                                 uint8_t *__restrict__ pt, float *__restrict__ ns) {
   const long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= R.ntot) return;
-  int c;
-  const long long p = split_index(R, s, c);
-  pt[R.pt_off + (long long)c * R.plane + p] = (uint8_t)pt_aos[s];
+  int c, h;
+  long long row;
+  const long long p = split_index(R, s, c, row, h);
+  const long long pp = row * R.hps + h;
+  pt[R.pt_off + (long long)c * R.pplane + pp] = (uint8_t)pt_aos[s];
   if (ns != nullptr) {
     float *d = ns + R.ns_off + (long long)(c * 3) * R.plane + p;
     d[0] = ns_aos ? ns_aos[3 * s] : 0.f;
@@ -614,9 +1077,11 @@ __global__ void k_split_to_mask(RepDev R, const uint8_t *__restrict__ pt, const 
                                 int *__restrict__ pt_aos, float *__restrict__ ns_aos) {
   const long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= R.ntot) return;
-  int c;
-  const long long p = split_index(R, s, c);
-  pt_aos[s] = pt ? pt[R.pt_off + (long long)c * R.plane + p] : 1;
+  int c, h;
+  long long row;
+  const long long p = split_index(R, s, c, row, h);
+  const long long pp = row * R.hps + h;
+  pt_aos[s] = pt ? pt[R.pt_off + (long long)c * R.pplane + pp] : 1;
   const float *d = ns ? ns + R.ns_off + (long long)(c * 3) * R.plane + p : nullptr;
   ns_aos[3 * s] = d ? d[0] : 0.f;
   ns_aos[3 * s + 1] = d ? d[R.plane] : 0.f;
@@ -630,9 +1095,11 @@ __global__ void k_init(RepDev R, const uint8_t *__restrict__ pt, float *__restri
                        float fx, float fy, float fz) {
   const long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= R.ntot) return;
-  int c;
-  const long long p = split_index(R, s, c);
-  const bool active = pt == nullptr || pt[R.pt_off + (long long)c * R.plane + p] != 0;
+  int c, h;
+  long long row;
+  const long long p = split_index(R, s, c, row, h);
+  const long long pp = row * R.hps + h;
+  const bool active = pt == nullptr || pt[R.pt_off + (long long)c * R.pplane + pp] != 0;
   float x = 0.f, y = 0.f, z = 1.f;
   if (active) {
     if (mode == 0) {
@@ -682,6 +1149,65 @@ static void launch_pass_p(const Variant &v, int mode, const PassArgs &a, int nbl
 void launch_pass(const Variant &v, int mode, const PassArgs &a, int nblocks, cudaStream_t st) {
   if (v.pot == POT_LL) launch_pass_p<POT_LL>(v, mode, a, nblocks, st);
   else launch_pass_p<POT_GHRL>(v, mode, a, nblocks, st);
+}
+
+template <int POT, bool MASK, bool FIELD>
+static void tpass_pmf(int mode, const PassArgs &a, int grid, int smem, cudaStream_t st) {
+  switch (mode) {
+    case MODE_SWEEP: k_tpass<POT, MASK, FIELD, MODE_SWEEP><<<grid, kBlock, smem, st>>>(a); break;
+    case MODE_SWEEP_MEASURE: k_tpass<POT, MASK, FIELD, MODE_SWEEP_MEASURE><<<grid, kBlock, smem, st>>>(a); break;
+    default: k_tpass<POT, MASK, FIELD, MODE_TRACE><<<grid, kBlock, smem, st>>>(a); break;
+  }
+}
+
+template <int POT, bool MASK, bool FIELD>
+static const void *tpass_fn(int mode) {
+  switch (mode) {
+    case MODE_SWEEP: return (const void *)k_tpass<POT, MASK, FIELD, MODE_SWEEP>;
+    case MODE_SWEEP_MEASURE: return (const void *)k_tpass<POT, MASK, FIELD, MODE_SWEEP_MEASURE>;
+    default: return (const void *)k_tpass<POT, MASK, FIELD, MODE_TRACE>;
+  }
+}
+
+static const void *tpass_select(const Variant &v, int mode) {
+  if (v.pot == POT_LL) {
+    if (v.mask) return v.field ? tpass_fn<POT_LL, true, true>(mode) : tpass_fn<POT_LL, true, false>(mode);
+    return v.field ? tpass_fn<POT_LL, false, true>(mode) : tpass_fn<POT_LL, false, false>(mode);
+  }
+  if (v.mask) return v.field ? tpass_fn<POT_GHRL, true, true>(mode) : tpass_fn<POT_GHRL, true, false>(mode);
+  return v.field ? tpass_fn<POT_GHRL, false, true>(mode) : tpass_fn<POT_GHRL, false, false>(mode);
+}
+
+int tpass_smem_bytes(int stage_bytes) { return kStages * stage_bytes; }
+
+int tpass_blocks_per_sm(const Variant &v, int mode, int stage_bytes) {
+  const void *fn = tpass_select(v, mode);
+  const int smem = tpass_smem_bytes(stage_bytes);
+  if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess) return 0;
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, kBlock, smem) != cudaSuccess) return 0;
+  return n;
+}
+
+void launch_tpass(const Variant &v, int mode, const PassArgs &a, int grid, cudaStream_t st) {
+  const int smem = tpass_smem_bytes(a.stage_bytes);
+  if (v.pot == POT_LL) {
+    if (v.mask) {
+      if (v.field) tpass_pmf<POT_LL, true, true>(mode, a, grid, smem, st);
+      else tpass_pmf<POT_LL, true, false>(mode, a, grid, smem, st);
+    } else {
+      if (v.field) tpass_pmf<POT_LL, false, true>(mode, a, grid, smem, st);
+      else tpass_pmf<POT_LL, false, false>(mode, a, grid, smem, st);
+    }
+  } else {
+    if (v.mask) {
+      if (v.field) tpass_pmf<POT_GHRL, true, true>(mode, a, grid, smem, st);
+      else tpass_pmf<POT_GHRL, true, false>(mode, a, grid, smem, st);
+    } else {
+      if (v.field) tpass_pmf<POT_GHRL, false, true>(mode, a, grid, smem, st);
+      else tpass_pmf<POT_GHRL, false, false>(mode, a, grid, smem, st);
+    }
+  }
 }
 
 void launch_flush(const FlushArgs &f, int nrep, cudaStream_t st) {

@@ -41,6 +41,11 @@ struct PassArgs {
   float *tr_dE;
   uint8_t *tr_acc;
   float *tr_prop;
+  // staged pass: the flat tile list and the shared-memory stage size
+  const int4 *tiles;  // (replica, j0, k0, 0)
+  int ntiles;
+  int stage_bytes;
+  unsigned *err;  // set to 1 when a shared-memory copy did not arrive in time
 };
 
 struct FlushArgs {
@@ -55,6 +60,12 @@ struct FlushArgs {
 };
 
 void launch_pass(const Variant &v, int mode, const PassArgs &a, int nblocks, cudaStream_t st);
+// The staged (TMA) pass over a.tiles with `grid` persistent CTAs.
+void launch_tpass(const Variant &v, int mode, const PassArgs &a, int grid, cudaStream_t st);
+// Dynamic shared memory of the staged pass for a stage size, and the CTAs
+// per SM it reaches (0 if it cannot run).
+int tpass_smem_bytes(int stage_bytes);
+int tpass_blocks_per_sm(const Variant &v, int mode, int stage_bytes);
 void launch_flush(const FlushArgs &f, int nrep, cudaStream_t st);
 void launch_measure_out(const RepDev *reps, double *ring, int ring_cap, int nrep, double *out, cudaStream_t st);
 void launch_aos_to_split(const RepDev &R, const float *aos, float *dir, cudaStream_t st);

@@ -127,6 +127,11 @@ def lib() -> C.CDLL:
         L.mcx_kernel_launches.argtypes = [V]
         L.mcx_kernel_launches.restype = C.c_longlong
         L.mcx_run_file.argtypes = [C.c_char_p, C.c_char_p]
+        L.mcx_set_staged.argtypes = [V, I]
+        L.mcx_get_staged.argtypes = [V]
+        L.mcx_stream.argtypes = [V]
+        L.mcx_stream.restype = V
+        L.mcx_pass_timing.argtypes = [V, I, C.POINTER(F), C.POINTER(F)]
         _lib = L
     return _lib
 
@@ -258,6 +263,14 @@ class Engine:
         prop = np.zeros((n, 3), np.float32)
         self._ck(self._L.mcx_debug_pass(self._h, r, colour, _p(dE), _p(acc), _p(prop)))
         return dE, acc, prop
+
+    @property
+    def staged(self) -> bool:
+        return bool(self._L.mcx_get_staged(self._h))
+
+    @staged.setter
+    def staged(self, on: bool):
+        self._ck(self._L.mcx_set_staged(self._h, 1 if on else 0))
 
     @property
     def kernel_launches(self) -> int:
