@@ -231,6 +231,31 @@ mcx_status mcx_read_geometry(const char *path, int nx, int ny, int nz, int *pt, 
  * it; desc (may be NULL) receives replica 0's descriptor. */
 mcx_status mcx_check_file(const char *param_file, mcx_replica_desc *desc);
 
+/* Allocation-free measurement (no counterpart in the reference: a GB300
+ * addition).  Some callers cannot allocate device memory when they need a
+ * measurement -- a framework that owns every device allocation through its
+ * own pool, or a latency-critical loop where cudaMalloc would synchronise the
+ * device.  This computes the mcx_measure layout (MCX_MEASURE_LEN doubles, in
+ * device memory at d_out) for a director field the caller already holds on
+ * the device: d_ni_aos is 3 floats per site in the reference's AoS order;
+ * d_pt (ints, NULL = every site active bulk) and d_ns_aos (NULL = zero
+ * normals) likewise.  Boundaries are desc's, forced by its geometry as
+ * mcx_create does.  It calls no cudaMalloc, cudaFree or allocating library
+ * routine: its only working memory is a fixed file-scope device array of
+ * MCX_NOALLOC_MAX_BLOCKS x 8 doubles plus a counter (68 KB), present on every
+ * GPU that loads the library until the process exits.  The first call on a
+ * device (made with that device current) looks up the array's device address
+ * with cudaGetSymbolAddress; make that first call before any stream capture.
+ * Every call shares the array: calls whose kernels overlap on the GPU (for
+ * example on two streams at once) race and give wrong results; calls ordered
+ * on one stream are safe.  Lattices above MCX_NOALLOC_MAX_SITES sites are
+ * rejected with MCX_ERR_INVALID.  Asynchronous on `stream` (a cudaStream_t,
+ * NULL = the default stream). */
+#define MCX_NOALLOC_MAX_BLOCKS 1024
+#define MCX_NOALLOC_MAX_SITES (1 << 27)
+mcx_status mcx_measure_noalloc(const mcx_replica_desc *desc, const float *d_ni_aos, const int *d_pt,
+                               const float *d_ns_aos, double *d_out, void *stream);
+
 /* ./mc_sim <param_file> (src/main.cpp:63-83): reads the reference's parameter
  * file (src/io.cpp:81-253), runs the selected mode on the GPU and writes
  * po.dat and director_field_*.csv into out_dir (NULL: current directory). */
