@@ -60,7 +60,8 @@ struct mcx_engine {
   std::vector<int4> tiles;  // (replica, j0, k0, 0)
   int4 *d_tiles = nullptr;
   int stage_bytes = 0;
-  int grid[2] = {0, 0};     // persistent CTAs for [measure]
+  int grid[2] = {0, 0};     // persistent CTAs of the staged pass for [measure]
+  int pgrid[4] = {0, 0, 0, 0};  // persistent CTAs of the direct pass per PassMode
   unsigned *d_err = nullptr;
 };
 
@@ -267,7 +268,7 @@ extern "C" mcx_status mcx_create(int n, const mcx_replica_desc *descs, mcx_engin
     if (d.elecA != 0.f) e->var.field = true;
     e->max_sites = std::max(e->max_sites, (long long)R.ntot);
     R.ncta = 0;
-    for (long long b = 0; b < R.npair; b += kBlock) {
+    for (long long b = 0; b < R.npair; b += pass_block_threads()) {
       e->map.push_back(make_int2(r, (int)b));
       R.ncta++;
     }
@@ -324,6 +325,20 @@ extern "C" mcx_status mcx_create(int n, const mcx_replica_desc *descs, mcx_engin
   CKC(cudaMalloc(&e->d_mout, sizeof(double) * 16 * n));
   CKC(cudaMalloc(&e->d_err, sizeof(unsigned)));
   CKC(cudaMemsetAsync(e->d_err, 0, sizeof(unsigned), e->stream));
+  {
+    int dev = 0, nsm = 0;
+    CKC(cudaGetDevice(&dev));
+    CKC(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    for (int m = 0; m < 4; m++) {
+      const int per = pass_blocks_per_sm(e->var, m);
+      if (per <= 0) {
+        st = fail(nullptr, MCX_ERR_CUDA, "direct pass kernel cannot be resident (occupancy 0)");
+        free_engine(e);
+        return st;
+      }
+      e->pgrid[m] = (int)std::min<long long>((long long)per * nsm, (long long)e->map.size());
+    }
+  }
   if (e->can_stage) {
     CKC(cudaMalloc(&e->d_tiles, sizeof(int4) * e->tiles.size()));
     CKC(cudaMemcpyAsync(e->d_tiles, e->tiles.data(), sizeof(int4) * e->tiles.size(), cudaMemcpyHostToDevice, e->stream));
@@ -536,6 +551,7 @@ static PassArgs pass_args(mcx_engine *e) {
   pa.stats = e->d_stats;
   pa.ring = e->d_ring;
   pa.ring_cap = e->ring_cap;
+  pa.nmap = (int)e->map.size();
   pa.tiles = e->d_tiles;
   pa.ntiles = (int)e->tiles.size();
   pa.stage_bytes = e->stage_bytes;
@@ -548,7 +564,7 @@ static void launch_sweep_pass(mcx_engine *e, PassArgs &pa, int colour, bool meas
   pa.colour = colour;
   const int mode = measure ? MODE_SWEEP_MEASURE : MODE_SWEEP;
   if (e->staged) launch_tpass(e->var, mode, pa, e->grid[measure ? 1 : 0], e->stream);
-  else launch_pass(e->var, mode, pa, (int)e->map.size(), e->stream);
+  else launch_pass(e->var, mode, pa, e->pgrid[mode], e->stream);
 }
 
 // One sweep's kernels on e->stream: the two colours.
@@ -654,7 +670,7 @@ extern "C" mcx_status mcx_measure(mcx_engine *e, int r, double *out) {
   PassArgs pa = pass_args(e);
   for (int c = 0; c < 2; c++) {
     pa.colour = c;
-    launch_pass(e->var, MODE_MEASURE_ONLY, pa, (int)e->map.size(), e->stream);
+    launch_pass(e->var, MODE_MEASURE_ONLY, pa, e->pgrid[MODE_MEASURE_ONLY], e->stream);
   }
   launch_measure_out(e->d_rep, e->d_ring, e->ring_cap, e->nrep, e->d_mout, e->stream);
   e->launches += 3;
@@ -814,7 +830,8 @@ extern "C" mcx_status mcx_debug_pass(mcx_engine *e, int r, int colour, float *dE
     pa.ntiles = Rr.ntile;
     launch_tpass(e->var, MODE_TRACE, pa, std::min(e->grid[0], Rr.ntile), e->stream);
   } else {
-    launch_pass(e->var, MODE_TRACE, pa, (int)sub.size(), e->stream);
+    pa.nmap = (int)sub.size();
+    launch_pass(e->var, MODE_TRACE, pa, std::min(e->pgrid[MODE_TRACE], (int)sub.size()), e->stream);
   }
   e->launches += 1;
   CKL(e);

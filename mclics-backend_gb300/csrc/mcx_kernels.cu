@@ -24,9 +24,10 @@
 #include "mcx_device.cuh"
 #include "mcx_kernels.cuh"
 
-// CTAs per SM the pass kernel is compiled for (caps its registers).
+// Threads and CTAs per SM the direct pass kernel is compiled for.
+constexpr int kPB = 128;
 #ifndef MCX_PASS_MIN_BLOCKS
-#define MCX_PASS_MIN_BLOCKS 3
+#define MCX_PASS_MIN_BLOCKS 5
 #endif
 
 namespace mcx {
@@ -186,169 +187,31 @@ __device__ __forceinline__ unsigned site_update(const RepDev &R, const PassArgs 
   return acc;
 }
 
-template <int POT, bool MASK, bool FIELD, int MODE>
-__global__ void __launch_bounds__(kBlock, MCX_PASS_MIN_BLOCKS) k_pass(PassArgs a) {
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// Block-wide, NT threads: adds this CTA's acceptance and measurement sums for
+// replica r, counts `units` finished work units (map entries or tiles) out of
+// the replica's `total`, and lets the CTA that finishes the replica's last
+// unit of a colour-1 sweep pass apply the step-size rule and advance the sweep
+// counters.  Sums stay FP32 inside the CTA; one FP64 atomic per quantity.
+template <int NT, int MODE>
+__device__ __forceinline__ void flush_replica(const PassArgs &a, int r, int units, unsigned total, unsigned acc,
+                                              float qs[kQ], bool mask) {
   constexpr bool MEAS = MODE == MODE_SWEEP_MEASURE || MODE == MODE_MEASURE_ONLY;
-  constexpr bool UPD = MODE != MODE_MEASURE_ONLY;
-  constexpr bool TRACE = MODE == MODE_TRACE;
-  const int2 m = a.map[blockIdx.x];
-  const RepDev &R = a.reps[m.x];
-  RepState *S = a.st + m.x;
-  const int c = a.colour;
-  const int t = m.y + (int)threadIdx.x;  // same-colour pair index
-  float qs[kQ];
-#pragma unroll
-  for (int q = 0; q < kQ; q++) qs[q] = 0.f;
-  unsigned acc = 0;
-  if (t < R.npair) {
-    const int hx = R.hx, ny = R.ny, nz = R.nz, hs = R.hs, P = R.plane;
-    const int row = (int)fastdiv((uint32_t)t, R.hp_m, R.hp_p);
-    const int h0 = 2 * (t - row * R.hp);
-    const int k = (int)fastdiv((uint32_t)row, R.ny_m, R.ny_p);
-    const int j = row - k * ny;
-    const int s = (c + j + k) & 1;
-    const bool hasB = h0 + 1 < hx;
-    const int off = row * hs + h0;
-    float *Ac = a.dir + R.dir_off + (long long)(c * 3) * P;
-    const float *Oc = a.dir + R.dir_off + (long long)((c ^ 1) * 3) * P;
-    const uint8_t *pa = a.pt + R.pt_off + (long long)c * R.pplane;
-    const uint8_t *po = a.pt + R.pt_off + (long long)(c ^ 1) * R.pplane;
-    const int offp = row * R.hps + h0;
-    // own pair and the other colour's pair at the same position
-    float2 ax = *reinterpret_cast<const float2 *>(Ac + off);
-    float2 ay = *reinterpret_cast<const float2 *>(Ac + off + P);
-    float2 az = *reinterpret_cast<const float2 *>(Ac + off + 2 * P);
-    const float2 ox = __ldg(reinterpret_cast<const float2 *>(Oc + off));
-    const float2 oy = __ldg(reinterpret_cast<const float2 *>(Oc + off + P));
-    const float2 oz = __ldg(reinterpret_cast<const float2 *>(Oc + off + 2 * P));
-    // the one other-colour site the pair's x bonds need beyond the pair:
-    // h0 - 1 when s = 0; when s = 1, h0 + 2, or h0 + 1 for a lone last site;
-    // wrapped at the row ends when x is periodic, absent when free
-    int exh;
-    float exe = 1.f;
-    if (s == 0) {
-      exh = h0 - 1;
-      if (exh < 0) { if (R.xb == BOUND_PERIODIC) exh = hx - 1; else exe = 0.f; }
-    } else {
-      exh = hasB ? h0 + 2 : h0 + 1;
-      if (exh == hx) { if (R.xb == BOUND_PERIODIC) exh = 0; else exe = 0.f; }
-    }
-    const int exo = exe != 0.f ? row * hs + exh : off;
-    const float ex = __ldg(Oc + exo), ey = __ldg(Oc + exo + P), ez = __ldg(Oc + exo + 2 * P);
-    // y+-, z+- rows of the other colour at the same h
-    float er[4] = {1.f, 1.f, 1.f, 1.f};
-    int rr[4] = {row + 1, row - 1, row + ny, row - ny};
-    if (j + 1 == ny) { if (R.yb == BOUND_PERIODIC) rr[0] -= ny; else er[0] = 0.f; }
-    if (j == 0) { if (R.yb == BOUND_PERIODIC) rr[1] += ny; else er[1] = 0.f; }
-    if (k + 1 == nz) { if (R.zb == BOUND_PERIODIC) rr[2] -= ny * nz; else er[2] = 0.f; }
-    if (k == 0) { if (R.zb == BOUND_PERIODIC) rr[3] += ny * nz; else er[3] = 0.f; }
-    float2 nr[4][3];
-    uchar2 pr[4];
-#pragma unroll
-    for (int d = 0; d < 4; d++) {
-      const int ro = er[d] != 0.f ? rr[d] * hs + h0 : off;
-      nr[d][0] = __ldg(reinterpret_cast<const float2 *>(Oc + ro));
-      nr[d][1] = __ldg(reinterpret_cast<const float2 *>(Oc + ro + P));
-      nr[d][2] = __ldg(reinterpret_cast<const float2 *>(Oc + ro + 2 * P));
-      if (MASK) pr[d] = __ldg(reinterpret_cast<const uchar2 *>(po + (er[d] != 0.f ? rr[d] * R.hps + h0 : offp)));
-    }
-    uchar2 pself2 = make_uchar2(1, 1), po2 = make_uchar2(1, 1);
-    uint8_t pex = 1;
-    if (MASK) {
-      pself2 = __ldg(reinterpret_cast<const uchar2 *>(pa + offp));
-      po2 = __ldg(reinterpret_cast<const uchar2 *>(po + offp));
-      pex = __ldg(po + (exe != 0.f ? row * R.hps + exh : offp));
-    }
-    float uA[3] = {0.f, 0.f, 0.f}, uB[3] = {0.f, 0.f, 0.f};
-    float ang = 0.f, invT = 0.f;
-    if (UPD) {
-      const unsigned long long sw = S->sweep;
-      const uint4 rw = philox4x32_10(make_uint4((uint32_t)t, (uint32_t)sw, (uint32_t)(sw >> 32), TAG_PLAIN | (uint32_t)c),
-                                     R.seed, R.stream);
-      pair_uniforms(rw, uA, uB);
-      ang = S->ang_var;
-      invT = 1.0f / S->T;
-    }
-    // weights: bond present (e) and neighbour active (w)
-    auto wt = [&](float ee, uint8_t p) { return MASK ? (ee != 0.f && p != 0 ? 1.f : 0.f) : ee; };
-    float nb[6][3], w[6], e[6];
-    // ---- site A (h0) ----
-    {
-      if (s == 0) {
-        nb[0][0] = ox.x; nb[0][1] = oy.x; nb[0][2] = oz.x; e[0] = 1.f; w[0] = wt(1.f, po2.x);
-        nb[1][0] = ex; nb[1][1] = ey; nb[1][2] = ez; e[1] = exe; w[1] = wt(exe, pex);
-      } else {
-        if (hasB) {
-          nb[0][0] = ox.y; nb[0][1] = oy.y; nb[0][2] = oz.y; e[0] = 1.f; w[0] = wt(1.f, po2.y);
-        } else {
-          nb[0][0] = ex; nb[0][1] = ey; nb[0][2] = ez; e[0] = exe; w[0] = wt(exe, pex);
-        }
-        nb[1][0] = ox.x; nb[1][1] = oy.x; nb[1][2] = oz.x; e[1] = 1.f; w[1] = wt(1.f, po2.x);
-      }
-#pragma unroll
-      for (int d = 0; d < 4; d++) {
-        nb[2 + d][0] = nr[d][0].x; nb[2 + d][1] = nr[d][1].x; nb[2 + d][2] = nr[d][2].x;
-        e[2 + d] = er[d];
-        w[2 + d] = wt(er[d], MASK ? pr[d].x : 1);
-      }
-      const int ps = MASK ? pself2.x : 1;
-      float sx = 0.f, sy = 0.f, sz = 0.f;
-      if (MASK && ps > 1) {
-        const float *nsb = a.ns + R.ns_off + (long long)(c * 3) * P + off;
-        sx = __ldg(nsb);
-        sy = __ldg(nsb + P);
-        sz = __ldg(nsb + 2 * P);
-      }
-      const uint32_t nat = (uint32_t)(2 * h0 + s) + (uint32_t)R.nx * (uint32_t)row;
-      acc += site_update<POT, MASK, FIELD, MODE>(R, a, c, ax.x, ay.x, az.x, nb, w, e, ps, sx, sy, sz, uA, ang, invT,
-                                                 nat, qs);
-    }
-    // ---- site B (h0 + 1) ----
-    if (hasB) {
-      if (s == 0) {
-        nb[0][0] = ox.y; nb[0][1] = oy.y; nb[0][2] = oz.y; e[0] = 1.f; w[0] = wt(1.f, po2.y);
-        nb[1][0] = ox.x; nb[1][1] = oy.x; nb[1][2] = oz.x; e[1] = 1.f; w[1] = wt(1.f, po2.x);
-      } else {
-        nb[0][0] = ex; nb[0][1] = ey; nb[0][2] = ez; e[0] = exe; w[0] = wt(exe, pex);
-        nb[1][0] = ox.y; nb[1][1] = oy.y; nb[1][2] = oz.y; e[1] = 1.f; w[1] = wt(1.f, po2.y);
-      }
-#pragma unroll
-      for (int d = 0; d < 4; d++) {
-        nb[2 + d][0] = nr[d][0].y; nb[2 + d][1] = nr[d][1].y; nb[2 + d][2] = nr[d][2].y;
-        e[2 + d] = er[d];
-        w[2 + d] = wt(er[d], MASK ? pr[d].y : 1);
-      }
-      const int ps = MASK ? pself2.y : 1;
-      float sx = 0.f, sy = 0.f, sz = 0.f;
-      if (MASK && ps > 1) {
-        const float *nsb = a.ns + R.ns_off + (long long)(c * 3) * P + off + 1;
-        sx = __ldg(nsb);
-        sy = __ldg(nsb + P);
-        sz = __ldg(nsb + 2 * P);
-      }
-      const uint32_t nat = (uint32_t)(2 * h0 + 2 + s) + (uint32_t)R.nx * (uint32_t)row;
-      acc += site_update<POT, MASK, FIELD, MODE>(R, a, c, ax.y, ay.y, az.y, nb, w, e, ps, sx, sy, sz, uB, ang, invT,
-                                                 nat, qs);
-    }
-    if (UPD) {
-      *reinterpret_cast<float2 *>(Ac + off) = ax;
-      *reinterpret_cast<float2 *>(Ac + off + P) = ay;
-      *reinterpret_cast<float2 *>(Ac + off + 2 * P) = az;
-    }
-  }
-  // ---- block reductions (FP32 within the CTA, one FP64 atomic per quantity) ----
-  __shared__ unsigned s_acc[kBlock / 32];
-  __shared__ float s_q[kBlock / 32][kQ];
+  constexpr bool COUNT = MODE == MODE_SWEEP || MODE == MODE_SWEEP_MEASURE;
+  __shared__ unsigned s_acc[NT / 32];
+  __shared__ float s_q[NT / 32][kQ];
   __shared__ unsigned s_last;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  if (UPD && !TRACE) {
+  const RepDev &R = a.reps[r];
+  RepState *S = a.st + r;
+  if (COUNT) {
     const unsigned wa = __reduce_add_sync(0xffffffffu, acc);
     if (lane == 0) s_acc[wid] = wa;
   }
   if (MEAS) {
 #pragma unroll
     for (int q = 0; q < kQ; q++) {
-      if (!MASK && q == 1) continue;  // without masks E_valid's sum equals E_all's
       float v = qs[q];
 #pragma unroll
       for (int o2 = 16; o2 > 0; o2 >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o2);
@@ -357,27 +220,27 @@ __global__ void __launch_bounds__(kBlock, MCX_PASS_MIN_BLOCKS) k_pass(PassArgs a
   }
   __syncthreads();
   const int lane_slot = blockIdx.x % kLanes;
-  if (UPD && !TRACE && threadIdx.x == 0) {
+  if (COUNT && threadIdx.x == 0) {
     unsigned tot = 0;
 #pragma unroll
-    for (int w2 = 0; w2 < kBlock / 32; w2++) tot += s_acc[w2];
+    for (int w2 = 0; w2 < NT / 32; w2++) tot += s_acc[w2];
     if (tot) atomicAdd(&S->acc[lane_slot], tot);
     __threadfence();
   }
   if (MEAS && threadIdx.x < kQ) {
-    const int q = (!MASK && threadIdx.x == 1) ? 0 : threadIdx.x;
+    const int q = (!mask && threadIdx.x == 1) ? 0 : threadIdx.x;
     float v = 0.f;
 #pragma unroll
-    for (int w2 = 0; w2 < kBlock / 32; w2++) v += s_q[w2][q];
+    for (int w2 = 0; w2 < NT / 32; w2++) v += s_q[w2][q];
     const unsigned long long slot = MODE == MODE_MEASURE_ONLY ? (unsigned long long)a.ring_cap
                                                               : S->meas % (unsigned long long)a.ring_cap;
-    double *ring = a.ring + (((size_t)m.x * (a.ring_cap + 1) + slot) * kLanes + lane_slot) * kQ;
+    double *ring = a.ring + (((size_t)r * (a.ring_cap + 1) + slot) * kLanes + lane_slot) * kQ;
     atomicAdd(ring + threadIdx.x, (double)v);
     __threadfence();
   }
-  if ((MODE == MODE_SWEEP || MODE == MODE_SWEEP_MEASURE) && c == 1) {
+  if (COUNT && a.colour == 1) {
     __syncthreads();
-    if (threadIdx.x == 0) s_last = atomicAdd(&S->done, 1u) == (unsigned)(R.ncta - 1);
+    if (threadIdx.x == 0) s_last = atomicAdd(&S->done, (unsigned)units) + (unsigned)units == total;
     __syncthreads();
     if (s_last && threadIdx.x == 0) {
       __threadfence();
@@ -398,13 +261,249 @@ __global__ void __launch_bounds__(kBlock, MCX_PASS_MIN_BLOCKS) k_pass(PassArgs a
       S->sweep += 1;
       if (MODE == MODE_SWEEP_MEASURE) S->meas += 1;
       S->done = 0;
-      double *st = a.stats + (size_t)m.x * kStats;
+      double *st = a.stats + (size_t)r * kStats;
       st[7] += (double)tot;
       st[8] += 1.0;
       st[11] = (double)av;
       st[12] = (double)S->sweep;
     }
   }
+  __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
+// Direct pass: persistent CTAs walk the map (entries of kPB same-colour site
+// pairs); each thread keeps a two-stage cp.async pipeline of its own pairs'
+// neighbourhoods in shared memory, so the loads of its next pair fly while it
+// updates the current one.  Slots are private to a thread: no block barrier
+// between pairs.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void cp_async(void *dst, const void *src, int bytes, bool valid) {
+  if (bytes == 8)
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(smem_u32(dst)), "l"(src), "r"(valid ? 8 : 0)
+                 : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(smem_u32(dst)), "l"(src), "r"(valid ? 4 : 0)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+
+// Shared-memory slots of one stage, struct of arrays over the CTA's threads.
+template <bool MASK>
+struct PairStage {
+  float2 v[18][kPB];  // own x y z, other colour same row x y z, rows y+ y- z+ z- (x y z each)
+  float ex[3][kPB];   // the extra other-colour site (x y z)
+  uint32_t pw[MASK ? 7 : 1][kPB];  // point-type words: own, other row, 4 rows, extra
+};
+
+// Where a thread's pair lives and who its neighbours are.
+struct PairGeom {
+  int row, h0, j, k, s, off, exh, offp;
+  bool valid, hasB;
+  float exe, er[4];
+  int rr[4];
+};
+
+__device__ __forceinline__ void pair_geom(const RepDev &R, int c, int t, PairGeom &g) {
+  g.valid = t < R.npair;
+  const int tt = g.valid ? t : 0;
+  g.row = (int)fastdiv((uint32_t)tt, R.hp_m, R.hp_p);
+  g.h0 = 2 * (tt - g.row * R.hp);
+  g.k = (int)fastdiv((uint32_t)g.row, R.ny_m, R.ny_p);
+  g.j = g.row - g.k * R.ny;
+  g.s = (c + g.j + g.k) & 1;
+  g.hasB = g.h0 + 1 < R.hx;
+  g.off = g.row * R.hs + g.h0;
+  g.offp = g.row * R.hps + g.h0;
+  g.exe = 1.f;
+  if (g.s == 0) {
+    g.exh = g.h0 - 1;
+    if (g.exh < 0) { if (R.xb == BOUND_PERIODIC) g.exh = R.hx - 1; else { g.exe = 0.f; g.exh = g.h0; } }
+  } else {
+    g.exh = g.hasB ? g.h0 + 2 : g.h0 + 1;
+    if (g.exh == R.hx) { if (R.xb == BOUND_PERIODIC) g.exh = 0; else { g.exe = 0.f; g.exh = g.h0; } }
+  }
+  const int ny = R.ny, nz = R.nz;
+  g.rr[0] = g.row + 1; g.rr[1] = g.row - 1; g.rr[2] = g.row + ny; g.rr[3] = g.row - ny;
+  g.er[0] = g.er[1] = g.er[2] = g.er[3] = 1.f;
+  if (g.j + 1 == ny) { if (R.yb == BOUND_PERIODIC) g.rr[0] -= ny; else { g.er[0] = 0.f; g.rr[0] = g.row; } }
+  if (g.j == 0) { if (R.yb == BOUND_PERIODIC) g.rr[1] += ny; else { g.er[1] = 0.f; g.rr[1] = g.row; } }
+  if (g.k + 1 == nz) { if (R.zb == BOUND_PERIODIC) g.rr[2] -= ny * nz; else { g.er[2] = 0.f; g.rr[2] = g.row; } }
+  if (g.k == 0) { if (R.zb == BOUND_PERIODIC) g.rr[3] += ny * nz; else { g.er[3] = 0.f; g.rr[3] = g.row; } }
+}
+
+template <bool MASK>
+__device__ __forceinline__ void prefetch_pair(const PassArgs &a, int c, int2 m, PairStage<MASK> &st) {
+  const RepDev &R = a.reps[m.x];
+  PairGeom g;
+  pair_geom(R, c, m.y + (int)threadIdx.x, g);
+  const int P = R.plane, tid = threadIdx.x;
+  const float *Ac = a.dir + R.dir_off + (long long)(c * 3) * P;
+  const float *Oc = a.dir + R.dir_off + (long long)((c ^ 1) * 3) * P;
+  const bool v = g.valid;
+#pragma unroll
+  for (int q = 0; q < 3; q++) {
+    cp_async(&st.v[q][tid], Ac + (long long)q * P + g.off, 8, v);
+    cp_async(&st.v[3 + q][tid], Oc + (long long)q * P + g.off, 8, v);
+    cp_async(&st.ex[q][tid], Oc + (long long)q * P + (long long)g.row * R.hs + g.exh, 4, v && g.exe != 0.f);
+#pragma unroll
+    for (int d = 0; d < 4; d++)
+      cp_async(&st.v[6 + 3 * d + q][tid], Oc + (long long)q * P + (long long)g.rr[d] * R.hs + g.h0, 8,
+               v && g.er[d] != 0.f);
+  }
+  if (MASK) {
+    // 4-byte words holding the needed point-type bytes (rows are 16-byte aligned)
+    const uint8_t *pa = a.pt + R.pt_off + (long long)c * R.pplane;
+    const uint8_t *po = a.pt + R.pt_off + (long long)(c ^ 1) * R.pplane;
+    cp_async(&st.pw[0][tid], pa + (g.offp & ~3), 4, v);
+    cp_async(&st.pw[1][tid], po + (g.offp & ~3), 4, v);
+#pragma unroll
+    for (int d = 0; d < 4; d++) cp_async(&st.pw[2 + d][tid], po + ((g.rr[d] * R.hps + g.h0) & ~3), 4, v && g.er[d] != 0.f);
+    cp_async(&st.pw[6][tid], po + ((g.row * R.hps + g.exh) & ~3), 4, v && g.exe != 0.f);
+  }
+}
+
+__device__ __forceinline__ uchar2 word_pair(uint32_t w, int byte) {
+  const uint32_t x = w >> (8 * byte);
+  return make_uchar2((uint8_t)(x & 0xFF), (uint8_t)((x >> 8) & 0xFF));
+}
+
+template <int POT, bool MASK, bool FIELD, int MODE>
+__device__ __forceinline__ void compute_pair(const PassArgs &a, int c, int2 m, const PairStage<MASK> &st, unsigned &acc,
+                                             float qs[kQ]) {
+  constexpr bool UPD = MODE != MODE_MEASURE_ONLY;
+  const RepDev &R = a.reps[m.x];
+  RepState *S = a.st + m.x;
+  PairGeom g;
+  pair_geom(R, c, m.y + (int)threadIdx.x, g);
+  if (!g.valid) return;
+  const int tid = threadIdx.x, P = R.plane;
+  float2 ax = st.v[0][tid], ay = st.v[1][tid], az = st.v[2][tid];
+  const float2 ox = st.v[3][tid], oy = st.v[4][tid], oz = st.v[5][tid];
+  const float ex = st.ex[0][tid], ey = st.ex[1][tid], ez = st.ex[2][tid];
+  uchar2 pself2 = make_uchar2(1, 1), po2 = make_uchar2(1, 1), pr[4];
+  uint8_t pex = 1;
+  if (MASK) {
+    const int b = g.offp & 3;
+    pself2 = word_pair(st.pw[0][tid], b);
+    po2 = word_pair(st.pw[1][tid], b);
+#pragma unroll
+    for (int d = 0; d < 4; d++) pr[d] = word_pair(st.pw[2 + d][tid], (g.rr[d] * R.hps + g.h0) & 3);
+    pex = (uint8_t)((st.pw[6][tid] >> (8 * ((g.row * R.hps + g.exh) & 3))) & 0xFF);
+  }
+  float uA[3] = {0.f, 0.f, 0.f}, uB[3] = {0.f, 0.f, 0.f};
+  float ang = 0.f, invT = 0.f;
+  if (UPD) {
+    const unsigned long long sw = S->sweep;
+    const uint32_t pid = (uint32_t)(m.y + tid);
+    const uint4 rw = philox4x32_10(make_uint4(pid, (uint32_t)sw, (uint32_t)(sw >> 32), TAG_PLAIN | (uint32_t)c),
+                                   R.seed, R.stream);
+    pair_uniforms(rw, uA, uB);
+    ang = S->ang_var;
+    invT = 1.0f / S->T;
+  }
+  auto wt = [&](float ee, uint8_t pp) { return MASK ? (ee != 0.f && pp != 0 ? 1.f : 0.f) : ee; };
+  float nb[6][3], w[6], e[6];
+  {
+    if (g.s == 0) {
+      nb[0][0] = ox.x; nb[0][1] = oy.x; nb[0][2] = oz.x; e[0] = 1.f; w[0] = wt(1.f, po2.x);
+      nb[1][0] = ex; nb[1][1] = ey; nb[1][2] = ez; e[1] = g.exe; w[1] = wt(g.exe, pex);
+    } else {
+      if (g.hasB) {
+        nb[0][0] = ox.y; nb[0][1] = oy.y; nb[0][2] = oz.y; e[0] = 1.f; w[0] = wt(1.f, po2.y);
+      } else {
+        nb[0][0] = ex; nb[0][1] = ey; nb[0][2] = ez; e[0] = g.exe; w[0] = wt(g.exe, pex);
+      }
+      nb[1][0] = ox.x; nb[1][1] = oy.x; nb[1][2] = oz.x; e[1] = 1.f; w[1] = wt(1.f, po2.x);
+    }
+#pragma unroll
+    for (int d = 0; d < 4; d++) {
+      const float2 X = st.v[6 + 3 * d][tid], Y = st.v[7 + 3 * d][tid], Z = st.v[8 + 3 * d][tid];
+      nb[2 + d][0] = X.x; nb[2 + d][1] = Y.x; nb[2 + d][2] = Z.x;
+      e[2 + d] = g.er[d];
+      w[2 + d] = wt(g.er[d], MASK ? pr[d].x : 1);
+    }
+    const int ps = MASK ? pself2.x : 1;
+    float sx = 0.f, sy = 0.f, sz = 0.f;
+    if (MASK && ps > 1) {
+      const float *nsb = a.ns + R.ns_off + (long long)(c * 3) * P + g.off;
+      sx = __ldg(nsb);
+      sy = __ldg(nsb + P);
+      sz = __ldg(nsb + 2 * P);
+    }
+    const uint32_t nat = (uint32_t)(2 * g.h0 + g.s) + (uint32_t)R.nx * (uint32_t)g.row;
+    acc += site_update<POT, MASK, FIELD, MODE>(R, a, c, ax.x, ay.x, az.x, nb, w, e, ps, sx, sy, sz, uA, ang, invT,
+                                               nat, qs);
+  }
+  if (g.hasB) {
+    if (g.s == 0) {
+      nb[0][0] = ox.y; nb[0][1] = oy.y; nb[0][2] = oz.y; e[0] = 1.f; w[0] = wt(1.f, po2.y);
+      nb[1][0] = ox.x; nb[1][1] = oy.x; nb[1][2] = oz.x; e[1] = 1.f; w[1] = wt(1.f, po2.x);
+    } else {
+      nb[0][0] = ex; nb[0][1] = ey; nb[0][2] = ez; e[0] = g.exe; w[0] = wt(g.exe, pex);
+      nb[1][0] = ox.y; nb[1][1] = oy.y; nb[1][2] = oz.y; e[1] = 1.f; w[1] = wt(1.f, po2.y);
+    }
+#pragma unroll
+    for (int d = 0; d < 4; d++) {
+      const float2 X = st.v[6 + 3 * d][tid], Y = st.v[7 + 3 * d][tid], Z = st.v[8 + 3 * d][tid];
+      nb[2 + d][0] = X.y; nb[2 + d][1] = Y.y; nb[2 + d][2] = Z.y;
+      e[2 + d] = g.er[d];
+      w[2 + d] = wt(g.er[d], MASK ? pr[d].y : 1);
+    }
+    const int ps = MASK ? pself2.y : 1;
+    float sx = 0.f, sy = 0.f, sz = 0.f;
+    if (MASK && ps > 1) {
+      const float *nsb = a.ns + R.ns_off + (long long)(c * 3) * P + g.off + 1;
+      sx = __ldg(nsb);
+      sy = __ldg(nsb + P);
+      sz = __ldg(nsb + 2 * P);
+    }
+    const uint32_t nat = (uint32_t)(2 * g.h0 + 2 + g.s) + (uint32_t)R.nx * (uint32_t)g.row;
+    acc += site_update<POT, MASK, FIELD, MODE>(R, a, c, ax.y, ay.y, az.y, nb, w, e, ps, sx, sy, sz, uB, ang, invT,
+                                               nat, qs);
+  }
+  if (UPD) {
+    float *gA = a.dir + R.dir_off + (long long)(c * 3) * P + g.off;
+    *reinterpret_cast<float2 *>(gA) = ax;
+    *reinterpret_cast<float2 *>(gA + P) = ay;
+    *reinterpret_cast<float2 *>(gA + 2 * P) = az;
+  }
+}
+
+template <int POT, bool MASK, bool FIELD, int MODE>
+__global__ void __launch_bounds__(kPB, MCX_PASS_MIN_BLOCKS) k_pass(PassArgs a) {
+  __shared__ PairStage<MASK> stages[2];
+  const int c = a.colour;
+  const int G = gridDim.x, n = a.nmap;
+  int e = blockIdx.x;
+  if (e < n) prefetch_pair<MASK>(a, c, a.map[e], stages[0]);
+  cp_async_commit();
+  int cur = -1, units = 0;
+  unsigned acc = 0;
+  float qs[kQ];
+#pragma unroll
+  for (int q = 0; q < kQ; q++) qs[q] = 0.f;
+  for (int it = 0; e < n; it++, e += G) {
+    const int2 m = a.map[e];
+    if (e + G < n) prefetch_pair<MASK>(a, c, a.map[e + G], stages[(it + 1) & 1]);
+    cp_async_commit();
+    if (m.x != cur) {
+      if (cur >= 0) {
+        flush_replica<kPB, MODE>(a, cur, units, (unsigned)a.reps[cur].ncta, acc, qs, MASK);
+        acc = 0;
+#pragma unroll
+        for (int q = 0; q < kQ; q++) qs[q] = 0.f;
+      }
+      cur = m.x;
+      units = 0;
+    }
+    cp_async_wait1();
+    compute_pair<POT, MASK, FIELD, MODE>(a, c, m, stages[it & 1], acc, qs);
+    units++;
+  }
+  asm volatile("cp.async.wait_all;" ::: "memory");
+  if (cur >= 0) flush_replica<kPB, MODE>(a, cur, units, (unsigned)a.reps[cur].ncta, acc, qs, MASK);
 }
 
 // ---------------------------------------------------------------------------
@@ -432,7 +531,6 @@ __global__ void __launch_bounds__(kBlock, MCX_PASS_MIN_BLOCKS) k_pass(PassArgs a
 constexpr int kStages = MCX_TPASS_STAGES;
 constexpr long long kWaitLimit = 1LL << 26;  // try_wait polls before giving up
 
-__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
 __device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
@@ -567,85 +665,6 @@ __device__ __forceinline__ void issue_tile(const PassArgs &a, int c, int t, char
     const uint32_t b = tile_copy<MASK>(a, R, c, td.y, td.z, v, i, d, sp);
     if (b) bulk_copy_g2s(d, sp, b, bar);
   }
-}
-
-// Block-wide: adds this CTA's acceptance and measurement sums for replica r,
-// counts `tiles` finished tiles, and lets the CTA that finishes the
-// replica's last tile of a colour-1 sweep pass apply the step-size rule.
-template <int MODE>
-__device__ __forceinline__ void flush_replica(const PassArgs &a, int r, int tiles, unsigned acc, float qs[kQ],
-                                              bool mask) {
-  constexpr bool MEAS = MODE == MODE_SWEEP_MEASURE;
-  constexpr bool TRACE = MODE == MODE_TRACE;
-  __shared__ unsigned s_acc[kBlock / 32];
-  __shared__ float s_q[kBlock / 32][kQ];
-  __shared__ unsigned s_last;
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const RepDev &R = a.reps[r];
-  RepState *S = a.st + r;
-  if (!TRACE) {
-    const unsigned wa = __reduce_add_sync(0xffffffffu, acc);
-    if (lane == 0) s_acc[wid] = wa;
-  }
-  if (MEAS) {
-#pragma unroll
-    for (int q = 0; q < kQ; q++) {
-      float v = qs[q];
-#pragma unroll
-      for (int o2 = 16; o2 > 0; o2 >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o2);
-      if (lane == 0) s_q[wid][q] = v;
-    }
-  }
-  __syncthreads();
-  const int lane_slot = blockIdx.x % kLanes;
-  if (!TRACE && threadIdx.x == 0) {
-    unsigned tot = 0;
-#pragma unroll
-    for (int w2 = 0; w2 < kBlock / 32; w2++) tot += s_acc[w2];
-    if (tot) atomicAdd(&S->acc[lane_slot], tot);
-    __threadfence();
-  }
-  if (MEAS && threadIdx.x < kQ) {
-    const int q = (!mask && threadIdx.x == 1) ? 0 : threadIdx.x;
-    float v = 0.f;
-#pragma unroll
-    for (int w2 = 0; w2 < kBlock / 32; w2++) v += s_q[w2][q];
-    const unsigned long long slot = S->meas % (unsigned long long)a.ring_cap;
-    double *ring = a.ring + (((size_t)r * (a.ring_cap + 1) + slot) * kLanes + lane_slot) * kQ;
-    atomicAdd(ring + threadIdx.x, (double)v);
-    __threadfence();
-  }
-  if (!TRACE && a.colour == 1) {
-    __syncthreads();
-    if (threadIdx.x == 0) s_last = atomicAdd(&S->done, (unsigned)tiles) + (unsigned)tiles == (unsigned)R.ntile;
-    __syncthreads();
-    if (s_last && threadIdx.x == 0) {
-      __threadfence();
-      unsigned tot = 0;
-#pragma unroll
-      for (int l = 0; l < kLanes; l++) tot += atomicExch(&S->acc[l], 0u);
-      // src/evolve.cpp:169-178 with the reference's float/double rounding
-      float av = S->ang_var;
-      const double ratio = 1.0 * (double)tot / (double)R.valid;
-      if (ratio < 0.5) {
-        av = (float)((double)av * 0.99);
-        if ((double)av < 0.01) av = (float)0.01;
-      } else if (ratio > 0.5) {
-        av = (float)((double)av / 0.99);
-        if ((double)av > 1.0) av = (float)((double)av - 0.5);
-      }
-      S->ang_var = av;
-      S->sweep += 1;
-      if (MEAS) S->meas += 1;
-      S->done = 0;
-      double *st = a.stats + (size_t)r * kStats;
-      st[7] += (double)tot;
-      st[8] += 1.0;
-      st[11] = (double)av;
-      st[12] = (double)S->sweep;
-    }
-  }
-  __syncthreads();
 }
 
 template <int POT, bool MASK, bool FIELD, int MODE>
@@ -821,7 +840,7 @@ __global__ void __launch_bounds__(kBlock, MCX_TPASS_MIN_BLOCKS) k_tpass(PassArgs
     const int4 td = a.tiles[t];
     if (td.x != cur) {
       if (cur >= 0) {
-        flush_replica<MODE>(a, cur, ntl, acc, qs, MASK);
+        flush_replica<kBlock, MODE>(a, cur, ntl, (unsigned)a.reps[cur].ntile, acc, qs, MASK);
         acc = 0;
 #pragma unroll
         for (int q = 0; q < kQ; q++) qs[q] = 0.f;
@@ -859,7 +878,7 @@ __global__ void __launch_bounds__(kBlock, MCX_TPASS_MIN_BLOCKS) k_tpass(PassArgs
     ntl++;
     __syncthreads();
   }
-  if (cur >= 0) flush_replica<MODE>(a, cur, ntl, acc, qs, MASK);
+  if (cur >= 0) flush_replica<kBlock, MODE>(a, cur, ntl, (unsigned)a.reps[cur].ntile, acc, qs, MASK);
 }
 
 // ---------------------------------------------------------------------------
@@ -1128,10 +1147,10 @@ __global__ void k_init(RepDev R, const uint8_t *__restrict__ pt, float *__restri
 template <int POT, bool MASK, bool FIELD>
 static void launch_pass_pmf(int mode, const PassArgs &a, int nblocks, cudaStream_t st) {
   switch (mode) {
-    case MODE_SWEEP: k_pass<POT, MASK, FIELD, MODE_SWEEP><<<nblocks, kBlock, 0, st>>>(a); break;
-    case MODE_SWEEP_MEASURE: k_pass<POT, MASK, FIELD, MODE_SWEEP_MEASURE><<<nblocks, kBlock, 0, st>>>(a); break;
-    case MODE_MEASURE_ONLY: k_pass<POT, MASK, FIELD, MODE_MEASURE_ONLY><<<nblocks, kBlock, 0, st>>>(a); break;
-    default: k_pass<POT, MASK, FIELD, MODE_TRACE><<<nblocks, kBlock, 0, st>>>(a); break;
+    case MODE_SWEEP: k_pass<POT, MASK, FIELD, MODE_SWEEP><<<nblocks, kPB, 0, st>>>(a); break;
+    case MODE_SWEEP_MEASURE: k_pass<POT, MASK, FIELD, MODE_SWEEP_MEASURE><<<nblocks, kPB, 0, st>>>(a); break;
+    case MODE_MEASURE_ONLY: k_pass<POT, MASK, FIELD, MODE_MEASURE_ONLY><<<nblocks, kPB, 0, st>>>(a); break;
+    default: k_pass<POT, MASK, FIELD, MODE_TRACE><<<nblocks, kPB, 0, st>>>(a); break;
   }
 }
 
@@ -1144,6 +1163,32 @@ static void launch_pass_p(const Variant &v, int mode, const PassArgs &a, int nbl
     if (v.field) launch_pass_pmf<POT, false, true>(mode, a, nblocks, st);
     else launch_pass_pmf<POT, false, false>(mode, a, nblocks, st);
   }
+}
+
+template <int POT, bool MASK, bool FIELD>
+static const void *pass_fn(int mode) {
+  switch (mode) {
+    case MODE_SWEEP: return (const void *)k_pass<POT, MASK, FIELD, MODE_SWEEP>;
+    case MODE_SWEEP_MEASURE: return (const void *)k_pass<POT, MASK, FIELD, MODE_SWEEP_MEASURE>;
+    case MODE_MEASURE_ONLY: return (const void *)k_pass<POT, MASK, FIELD, MODE_MEASURE_ONLY>;
+    default: return (const void *)k_pass<POT, MASK, FIELD, MODE_TRACE>;
+  }
+}
+
+int pass_block_threads() { return kPB; }
+
+int pass_blocks_per_sm(const Variant &v, int mode) {
+  const void *fn;
+  if (v.pot == POT_LL) {
+    if (v.mask) fn = v.field ? pass_fn<POT_LL, true, true>(mode) : pass_fn<POT_LL, true, false>(mode);
+    else fn = v.field ? pass_fn<POT_LL, false, true>(mode) : pass_fn<POT_LL, false, false>(mode);
+  } else {
+    if (v.mask) fn = v.field ? pass_fn<POT_GHRL, true, true>(mode) : pass_fn<POT_GHRL, true, false>(mode);
+    else fn = v.field ? pass_fn<POT_GHRL, false, true>(mode) : pass_fn<POT_GHRL, false, false>(mode);
+  }
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, kPB, 0) != cudaSuccess) return 0;
+  return n;
 }
 
 void launch_pass(const Variant &v, int mode, const PassArgs &a, int nblocks, cudaStream_t st) {

@@ -28,7 +28,8 @@ enum PassMode : int {
 
 struct PassArgs {
   const RepDev *reps;
-  const int2 *map;  // per CTA: (replica, first site of the colour)
+  const int2 *map;  // work units of the direct pass: (replica, first same-colour pair)
+  int nmap;
   float *dir;
   const uint8_t *pt;
   const float *ns;
@@ -59,7 +60,10 @@ struct FlushArgs {
   int count;                 // pending slots
 };
 
+// The direct pass over a.map with `nblocks` persistent CTAs.
 void launch_pass(const Variant &v, int mode, const PassArgs &a, int nblocks, cudaStream_t st);
+int pass_blocks_per_sm(const Variant &v, int mode);
+int pass_block_threads();
 // The staged (TMA) pass over a.tiles with `grid` persistent CTAs.
 void launch_tpass(const Variant &v, int mode, const PassArgs &a, int grid, cudaStream_t st);
 // Dynamic shared memory of the staged pass for a stage size, and the CTAs
