@@ -207,6 +207,31 @@ long long mcx_kernel_launches(const mcx_engine *eng);
 mcx_status mcx_set_staged(mcx_engine *eng, int on);
 int mcx_get_staged(const mcx_engine *eng);
 
+/* Learned proposal (no counterpart in the reference).  A small network reads
+ * a site's six neighbour directors and T (19 inputs) and gives the mean axis
+ * and log-concentration of an antipodal von Mises-Fisher mixture,
+ * q(n') = kappa/(4 pi sinh kappa) cosh(kappa mu.n'); sweeps with
+ * MCX_PROPOSAL_VMF_MLP draw n' from it and accept with the exact
+ * Metropolis-Hastings ratio exp(-dE/T) cosh(kappa mu.n)/cosh(kappa mu.n'),
+ * so the stationary distribution is the same as with the plain rotation
+ * (MCX_PROPOSAL_PLAIN, the default and the reference's move).
+ * Weights (MCX_MLP_PARAMS floats, row index = input):
+ *   W1 [32][64] (input rows 19..31 zero), b1 [64], W2 [64][64], b2 [64],
+ *   W3 [64][8] (output columns 4..7 zero), b3 [8];
+ * inputs are the neighbours x+ x- y+ y- z+ z- (3 each, zero when absent or
+ * inactive) then T; outputs mu (3) and log kappa (clamped to [-4, 6]).
+ * The network runs in BF16 with FP32 accumulation on the tensor cores. */
+typedef enum { MCX_PROPOSAL_PLAIN = 0, MCX_PROPOSAL_VMF_MLP = 1 } mcx_proposal;
+#define MCX_MLP_PARAMS 6792
+int mcx_mlp_params(void);
+mcx_status mcx_set_mlp(mcx_engine *eng, const float *weights, int n);
+mcx_status mcx_get_mlp(mcx_engine *eng, float *weights);
+mcx_status mcx_set_proposal(mcx_engine *eng, int kind);
+/* mcx_debug_pass plus, per site, the network's 4 outputs (learned proposal;
+ * mlp_out may be NULL). */
+mcx_status mcx_debug_pass_mlp(mcx_engine *eng, int replica, int colour, float *dE, unsigned char *acc,
+                              float *proposal_aos, float *mlp_out);
+
 /* The engine's CUDA stream (a cudaStream_t), for callers that record events
  * or order their own work against the engine's. */
 void *mcx_stream(mcx_engine *eng);

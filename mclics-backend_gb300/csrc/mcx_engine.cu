@@ -63,6 +63,11 @@ struct mcx_engine {
   int grid[2] = {0, 0};     // persistent CTAs of the staged pass for [measure]
   int pgrid[4] = {0, 0, 0, 0};  // persistent CTAs of the direct pass per PassMode
   unsigned *d_err = nullptr;
+  // learned proposal
+  int proposal = MCX_PROPOSAL_PLAIN;
+  uint8_t *d_mlp = nullptr;
+  std::vector<float> mlp;  // FP32 weights as last set or trained
+  int lgrid[4] = {0, 0, 0, 0};
 };
 
 static mcx_status fail(mcx_engine *e, mcx_status st, const char *fmt, ...) {
@@ -165,6 +170,7 @@ static void free_engine(mcx_engine *e) {
   cudaFree(e->d_stage_pt);
   cudaFree(e->d_tiles);
   cudaFree(e->d_err);
+  cudaFree(e->d_mlp);
   if (e->stream) cudaStreamDestroy(e->stream);
   delete e;
 }
@@ -552,6 +558,7 @@ static PassArgs pass_args(mcx_engine *e) {
   pa.ring = e->d_ring;
   pa.ring_cap = e->ring_cap;
   pa.nmap = (int)e->map.size();
+  pa.mlp = e->d_mlp;
   pa.tiles = e->d_tiles;
   pa.ntiles = (int)e->tiles.size();
   pa.stage_bytes = e->stage_bytes;
@@ -563,7 +570,8 @@ static PassArgs pass_args(mcx_engine *e) {
 static void launch_sweep_pass(mcx_engine *e, PassArgs &pa, int colour, bool measure) {
   pa.colour = colour;
   const int mode = measure ? MODE_SWEEP_MEASURE : MODE_SWEEP;
-  if (e->staged) launch_tpass(e->var, mode, pa, e->grid[measure ? 1 : 0], e->stream);
+  if (e->proposal == MCX_PROPOSAL_VMF_MLP) launch_pass_learned(e->var, mode, pa, e->lgrid[mode], e->stream);
+  else if (e->staged) launch_tpass(e->var, mode, pa, e->grid[measure ? 1 : 0], e->stream);
   else launch_pass(e->var, mode, pa, e->pgrid[mode], e->stream);
 }
 
@@ -663,6 +671,60 @@ extern "C" mcx_status mcx_set_staged(mcx_engine *e, int on) {
 }
 
 extern "C" int mcx_get_staged(const mcx_engine *e) { return e && e->staged ? 1 : 0; }
+
+static void drop_graphs(mcx_engine *e) {
+  for (int m = 0; m < 2; m++)
+    if (e->graph[m]) {
+      cudaGraphExecDestroy(e->graph[m]);
+      e->graph[m] = nullptr;
+    }
+}
+
+extern "C" int mcx_mlp_params(void) { return MCX_MLP_PARAMS; }
+
+extern "C" mcx_status mcx_set_mlp(mcx_engine *e, const float *w, int n) {
+  if (!e) return fail(nullptr, MCX_ERR_INVALID, "null engine");
+  if (!w || n != MCX_MLP_PARAMS) return fail(e, MCX_ERR_INVALID, "mcx_set_mlp: expected %d weights, got %d", MCX_MLP_PARAMS, n);
+  for (int i = 0; i < n; i++)
+    if (!(w[i] == w[i]) || w[i] > 1e30f || w[i] < -1e30f) return fail(e, MCX_ERR_INVALID, "mcx_set_mlp: weight %d is not finite", i);
+  std::vector<uint8_t> packed(mlp_device_bytes());
+  pack_mlp_weights(w, packed.data());
+  CK(e, cudaStreamSynchronize(e->stream));
+  if (!e->d_mlp) {
+    cudaError_t r = cudaMalloc(&e->d_mlp, packed.size());
+    if (r != cudaSuccess) return fail(e, MCX_ERR_NOMEM, "mcx_set_mlp: %s", cudaGetErrorString(r));
+    int dev = 0, nsm = 0;
+    CK(e, cudaGetDevice(&dev));
+    CK(e, cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    for (int m = 0; m < 4; m++) {
+      if (m == MODE_MEASURE_ONLY) continue;
+      const int per = pass_learned_blocks_per_sm(e->var, m);
+      if (per <= 0) return fail(e, MCX_ERR_CUDA, "learned pass kernel cannot be resident");
+      e->lgrid[m] = (int)std::min<long long>((long long)per * nsm, (long long)e->map.size());
+    }
+  }
+  CK(e, cudaMemcpy(e->d_mlp, packed.data(), packed.size(), cudaMemcpyHostToDevice));
+  e->mlp.assign(w, w + n);
+  drop_graphs(e);  // captured launches hold the weight pointer only, but keep it simple
+  return MCX_OK;
+}
+
+extern "C" mcx_status mcx_get_mlp(mcx_engine *e, float *w) {
+  if (!e || !w) return fail(e, MCX_ERR_INVALID, "mcx_get_mlp: null argument");
+  if (e->mlp.empty()) return fail(e, MCX_ERR_INVALID, "no network weights set");
+  memcpy(w, e->mlp.data(), sizeof(float) * e->mlp.size());
+  return MCX_OK;
+}
+
+extern "C" mcx_status mcx_set_proposal(mcx_engine *e, int kind) {
+  if (!e) return fail(nullptr, MCX_ERR_INVALID, "null engine");
+  if (kind != MCX_PROPOSAL_PLAIN && kind != MCX_PROPOSAL_VMF_MLP) return fail(e, MCX_ERR_INVALID, "unknown proposal %d", kind);
+  if (kind == MCX_PROPOSAL_VMF_MLP && !e->d_mlp) return fail(e, MCX_ERR_INVALID, "set the network weights (mcx_set_mlp) first");
+  CK(e, cudaStreamSynchronize(e->stream));
+  e->proposal = kind;
+  drop_graphs(e);
+  return MCX_OK;
+}
 
 extern "C" mcx_status mcx_measure(mcx_engine *e, int r, double *out) {
   if (mcx_status st = check_rep(e, r)) return st;
@@ -797,6 +859,11 @@ extern "C" mcx_status mcx_read_geometry(const char *path, int nx, int ny, int nz
 }
 
 extern "C" mcx_status mcx_debug_pass(mcx_engine *e, int r, int colour, float *dE, unsigned char *acc, float *prop) {
+  return mcx_debug_pass_mlp(e, r, colour, dE, acc, prop, nullptr);
+}
+
+extern "C" mcx_status mcx_debug_pass_mlp(mcx_engine *e, int r, int colour, float *dE, unsigned char *acc, float *prop,
+                                         float *mlp_out) {
   if (mcx_status st = check_rep(e, r)) return st;
   if (colour != 0 && colour != 1) return fail(e, MCX_ERR_INVALID, "colour must be 0 or 1");
   const RepDev &R = e->rep[r];
@@ -810,6 +877,11 @@ extern "C" mcx_status mcx_debug_pass(mcx_engine *e, int r, int colour, float *dE
   CK(e, cudaMalloc(&d_prop, sizeof(float) * 3 * R.ntot));
   CK(e, cudaMalloc(&d_acc, R.ntot));
   CK(e, cudaMalloc(&d_map, sizeof(int2) * sub.size()));
+  float *d_y = nullptr;
+  if (mlp_out) {
+    CK(e, cudaMalloc(&d_y, sizeof(float) * 4 * R.ntot));
+    CK(e, cudaMemsetAsync(d_y, 0, sizeof(float) * 4 * R.ntot, e->stream));
+  }
   CK(e, cudaMemsetAsync(d_dE, 0, sizeof(float) * R.ntot, e->stream));
   CK(e, cudaMemsetAsync(d_prop, 0, sizeof(float) * 3 * R.ntot, e->stream));
   CK(e, cudaMemsetAsync(d_acc, 0xFF, R.ntot, e->stream));
@@ -820,8 +892,12 @@ extern "C" mcx_status mcx_debug_pass(mcx_engine *e, int r, int colour, float *dE
   pa.tr_dE = d_dE;
   pa.tr_acc = d_acc;
   pa.tr_prop = d_prop;
+  pa.tr_y = d_y;
   int4 *d_sub_tiles = nullptr;
-  if (e->staged) {
+  if (e->proposal == MCX_PROPOSAL_VMF_MLP) {
+    pa.nmap = (int)sub.size();
+    launch_pass_learned(e->var, MODE_TRACE, pa, std::min(e->lgrid[MODE_TRACE], (int)sub.size()), e->stream);
+  } else if (e->staged) {
     const RepDev &Rr = e->rep[r];
     CK(e, cudaMalloc(&d_sub_tiles, sizeof(int4) * Rr.ntile));
     CK(e, cudaMemcpyAsync(d_sub_tiles, e->tiles.data() + Rr.tile0, sizeof(int4) * Rr.ntile, cudaMemcpyHostToDevice,
@@ -838,11 +914,13 @@ extern "C" mcx_status mcx_debug_pass(mcx_engine *e, int r, int colour, float *dE
   if (dE) CK(e, cudaMemcpyAsync(dE, d_dE, sizeof(float) * R.ntot, cudaMemcpyDeviceToHost, e->stream));
   if (acc) CK(e, cudaMemcpyAsync(acc, d_acc, R.ntot, cudaMemcpyDeviceToHost, e->stream));
   if (prop) CK(e, cudaMemcpyAsync(prop, d_prop, sizeof(float) * 3 * R.ntot, cudaMemcpyDeviceToHost, e->stream));
+  if (mlp_out) CK(e, cudaMemcpyAsync(mlp_out, d_y, sizeof(float) * 4 * R.ntot, cudaMemcpyDeviceToHost, e->stream));
   CK(e, cudaStreamSynchronize(e->stream));
   cudaFree(d_dE);
   cudaFree(d_prop);
   cudaFree(d_acc);
   cudaFree(d_map);
   cudaFree(d_sub_tiles);
+  cudaFree(d_y);
   return check_err_flag(e);
 }

@@ -23,488 +23,9 @@
 
 #include "mcx_device.cuh"
 #include "mcx_kernels.cuh"
-
-// Threads and CTAs per SM the direct pass kernel is compiled for.
-constexpr int kPB = 128;
-#ifndef MCX_PASS_MIN_BLOCKS
-#define MCX_PASS_MIN_BLOCKS 5
-#endif
+#include "mcx_pass.cuh"
 
 namespace mcx {
-
-// Bond energy of director a with neighbour b in slot d (x+, x-, y+, y-, z+, z-).
-template <int POT, int D>
-__device__ __forceinline__ float bond(const RepDev &R, float ax, float ay, float az, const float b[3]) {
-  if (POT == POT_LL) {
-    const float nij = ax * b[0] + ay * b[1] + az * b[2];
-    return -1.5f * R.A * nij * nij;
-  } else {
-    return ghrl_bond<(D >> 1)>(R, ax, ay, az, b[0], b[1], b[2], (D & 1) ? -1.f : 1.f);
-  }
-}
-
-// Weighted bond sum of director a over the six slots.  For LL the constant
-// -1.5 A is applied by the caller so that old and new sums share it.
-template <int POT>
-__device__ __forceinline__ float bond_sum(const RepDev &R, float ax, float ay, float az, const float nb[6][3],
-                                          const float w[6]) {
-  if (POT == POT_LL) {
-    float acc = 0.f;
-#pragma unroll
-    for (int d = 0; d < 6; d++) {
-      const float nij = ax * nb[d][0] + ay * nb[d][1] + az * nb[d][2];
-      acc = fmaf(nij * w[d], nij, acc);
-    }
-    return acc;
-  } else {
-    float acc = 0.f;
-    acc = fmaf(w[0], bond<POT, 0>(R, ax, ay, az, nb[0]), acc);
-    acc = fmaf(w[1], bond<POT, 1>(R, ax, ay, az, nb[1]), acc);
-    acc = fmaf(w[2], bond<POT, 2>(R, ax, ay, az, nb[2]), acc);
-    acc = fmaf(w[3], bond<POT, 3>(R, ax, ay, az, nb[3]), acc);
-    acc = fmaf(w[4], bond<POT, 4>(R, ax, ay, az, nb[4]), acc);
-    acc = fmaf(w[5], bond<POT, 5>(R, ax, ay, az, nb[5]), acc);
-    return acc;
-  }
-}
-
-template <int POT>
-__device__ __forceinline__ float bond_scale(const RepDev &R) {
-  return POT == POT_LL ? -1.5f * R.A : 1.f;
-}
-
-// Rotated proposal (src/evolve.cpp:136-152 / src/evolve.cu:143-163): rotate by
-// pi*va about x (u1 < 0.333), y (u1 < 0.666) or z, then renormalise.  Written
-// as one rotation of the component pair (u, v) = (y, z), (z, x) or (x, y):
-// u' = u c + v s, v' = v c - u s, which is the reference's three formulas.
-// sin and cos are taken of |angle| and the sign restored, so a move and its
-// reverse are exact mirror images (a symmetric proposal).
-__device__ __forceinline__ void propose(float x, float y, float z, float u0, float u1, float ang, float &px, float &py,
-                                        float &pz) {
-  const float va = (2.f * u0 - 1.f) * ang;
-  const float th = 3.14159265358979f * va;
-  const float at = fabsf(th);
-  const float sn = copysignf(__sinf(at), th);
-  const float cs = __cosf(at);
-  const int axis = u1 < 0.333f ? 0 : (u1 < 0.666f ? 1 : 2);
-  const float u = axis == 0 ? y : (axis == 1 ? z : x);
-  const float v = axis == 0 ? z : (axis == 1 ? x : y);
-  const float up = u * cs + v * sn;
-  const float vp = v * cs - u * sn;
-  px = axis == 0 ? x : (axis == 1 ? vp : up);
-  py = axis == 0 ? up : (axis == 1 ? y : vp);
-  pz = axis == 0 ? vp : (axis == 1 ? up : z);
-  const float inv = rsqrtf(px * px + py * py + pz * pz);
-  px *= inv;
-  py *= inv;
-  pz *= inv;
-}
-
-// One site update (and, in measured modes, its share of E and Q).  x, y, z
-// hold the site's director and receive the final one; nb / w are the six
-// neighbours and their update weights (bond present and neighbour active);
-// e marks bonds present whatever the neighbour's type.
-template <int POT, bool MASK, bool FIELD, int MODE>
-__device__ __forceinline__ unsigned site_update(const RepDev &R, const PassArgs &a, int c, float &x, float &y,
-                                                float &z, const float nb[6][3], const float w[6], const float e[6],
-                                                int pself, float sx, float sy, float sz, const float u[3], float ang,
-                                                float invT, uint32_t nat, float qs[kQ]) {
-  constexpr bool MEAS = MODE == MODE_SWEEP_MEASURE || MODE == MODE_MEASURE_ONLY;
-  constexpr bool UPD = MODE != MODE_MEASURE_ONLY;
-  constexpr bool TRACE = MODE == MODE_TRACE;
-  const int sid = pself - 2;
-  const bool surf = MASK && pself > 1 && sid < R.nsurf;
-  unsigned acc = 0;
-  float eb = 0.f;  // final bond sum to active neighbours (unscaled for LL)
-  if (pself != 0) {
-    const float b_old = bond_sum<POT>(R, x, y, z, nb, w);
-    eb = b_old;
-    if (UPD) {
-      float px, py, pz;
-      propose(x, y, z, u[0], u[1], ang, px, py, pz);
-      const float b_new = bond_sum<POT>(R, px, py, pz, nb, w);
-      float dE = bond_scale<POT>(R) * (b_new - b_old);
-      if (surf) dE += surface_energy(R, sid, px, py, pz, sx, sy, sz) - surface_energy(R, sid, x, y, z, sx, sy, sz);
-      if (FIELD) dE += field_energy(R, px, py, pz) - field_energy(R, x, y, z);
-      // src/evolve.cpp:160: accept when u < exp(-(E_new - E_old)/T)
-      const bool accept = u[2] < __expf(-dE * invT);
-      if (TRACE) {
-        a.tr_dE[nat] = dE;
-        a.tr_acc[nat] = accept ? 1 : 0;
-        a.tr_prop[3 * (size_t)nat] = px;
-        a.tr_prop[3 * (size_t)nat + 1] = py;
-        a.tr_prop[3 * (size_t)nat + 2] = pz;
-      }
-      if (accept) {
-        x = px;
-        y = py;
-        z = pz;
-        eb = b_new;
-        acc = 1;
-      }
-    }
-  } else if (TRACE) {
-    a.tr_dE[nat] = 0.f;
-    a.tr_acc[nat] = 255;
-  }
-  if (MEAS) {
-    const float act = pself != 0 ? 1.f : 0.f;
-    if (pself != 0) {
-      qs[2] += x * x;
-      qs[3] += x * y;
-      qs[4] += x * z;
-      qs[5] += y * y;
-      qs[6] += y * z;
-    }
-    if (surf) {
-      const float es = surface_energy(R, sid, x, y, z, sx, sy, sz);
-      qs[0] += es;
-      qs[1] += es;
-    }
-    if (FIELD) {
-      const float ef = field_energy(R, x, y, z);
-      qs[0] += ef;
-      qs[1] += act * ef;
-    }
-    if (c == 1) {
-      // each bond counts in the local energy of each active end; the
-      // all-site energy also counts inactive sites' bonds to active ones
-      if (pself != 0) {
-        const float ebs = bond_scale<POT>(R) * eb;
-        qs[0] += 2.f * ebs;
-        qs[1] += 2.f * ebs;
-        if (MASK) {
-          float wi[6];
-#pragma unroll
-          for (int d = 0; d < 6; d++) wi[d] = e[d] - w[d];
-          qs[0] += bond_scale<POT>(R) * bond_sum<POT>(R, x, y, z, nb, wi);
-        }
-      } else {
-        qs[0] += bond_scale<POT>(R) * bond_sum<POT>(R, x, y, z, nb, w);
-      }
-    }
-  }
-  return acc;
-}
-
-__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-// Block-wide, NT threads: adds this CTA's acceptance and measurement sums for
-// replica r, counts `units` finished work units (map entries or tiles) out of
-// the replica's `total`, and lets the CTA that finishes the replica's last
-// unit of a colour-1 sweep pass apply the step-size rule and advance the sweep
-// counters.  Sums stay FP32 inside the CTA; one FP64 atomic per quantity.
-template <int NT, int MODE>
-__device__ __forceinline__ void flush_replica(const PassArgs &a, int r, int units, unsigned total, unsigned acc,
-                                              float qs[kQ], bool mask) {
-  constexpr bool MEAS = MODE == MODE_SWEEP_MEASURE || MODE == MODE_MEASURE_ONLY;
-  constexpr bool COUNT = MODE == MODE_SWEEP || MODE == MODE_SWEEP_MEASURE;
-  __shared__ unsigned s_acc[NT / 32];
-  __shared__ float s_q[NT / 32][kQ];
-  __shared__ unsigned s_last;
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const RepDev &R = a.reps[r];
-  RepState *S = a.st + r;
-  if (COUNT) {
-    const unsigned wa = __reduce_add_sync(0xffffffffu, acc);
-    if (lane == 0) s_acc[wid] = wa;
-  }
-  if (MEAS) {
-#pragma unroll
-    for (int q = 0; q < kQ; q++) {
-      float v = qs[q];
-#pragma unroll
-      for (int o2 = 16; o2 > 0; o2 >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o2);
-      if (lane == 0) s_q[wid][q] = v;
-    }
-  }
-  __syncthreads();
-  const int lane_slot = blockIdx.x % kLanes;
-  if (COUNT && threadIdx.x == 0) {
-    unsigned tot = 0;
-#pragma unroll
-    for (int w2 = 0; w2 < NT / 32; w2++) tot += s_acc[w2];
-    if (tot) atomicAdd(&S->acc[lane_slot], tot);
-    __threadfence();
-  }
-  if (MEAS && threadIdx.x < kQ) {
-    const int q = (!mask && threadIdx.x == 1) ? 0 : threadIdx.x;
-    float v = 0.f;
-#pragma unroll
-    for (int w2 = 0; w2 < NT / 32; w2++) v += s_q[w2][q];
-    const unsigned long long slot = MODE == MODE_MEASURE_ONLY ? (unsigned long long)a.ring_cap
-                                                              : S->meas % (unsigned long long)a.ring_cap;
-    double *ring = a.ring + (((size_t)r * (a.ring_cap + 1) + slot) * kLanes + lane_slot) * kQ;
-    atomicAdd(ring + threadIdx.x, (double)v);
-    __threadfence();
-  }
-  if (COUNT && a.colour == 1) {
-    __syncthreads();
-    if (threadIdx.x == 0) s_last = atomicAdd(&S->done, (unsigned)units) + (unsigned)units == total;
-    __syncthreads();
-    if (s_last && threadIdx.x == 0) {
-      __threadfence();
-      unsigned tot = 0;
-#pragma unroll
-      for (int l = 0; l < kLanes; l++) tot += atomicExch(&S->acc[l], 0u);
-      // src/evolve.cpp:169-178 with the reference's float/double rounding
-      float av = S->ang_var;
-      const double ratio = 1.0 * (double)tot / (double)R.valid;
-      if (ratio < 0.5) {
-        av = (float)((double)av * 0.99);
-        if ((double)av < 0.01) av = (float)0.01;
-      } else if (ratio > 0.5) {
-        av = (float)((double)av / 0.99);
-        if ((double)av > 1.0) av = (float)((double)av - 0.5);
-      }
-      S->ang_var = av;
-      S->sweep += 1;
-      if (MODE == MODE_SWEEP_MEASURE) S->meas += 1;
-      S->done = 0;
-      double *st = a.stats + (size_t)r * kStats;
-      st[7] += (double)tot;
-      st[8] += 1.0;
-      st[11] = (double)av;
-      st[12] = (double)S->sweep;
-    }
-  }
-  __syncthreads();
-}
-
-// ---------------------------------------------------------------------------
-// Direct pass: persistent CTAs walk the map (entries of kPB same-colour site
-// pairs); each thread keeps a two-stage cp.async pipeline of its own pairs'
-// neighbourhoods in shared memory, so the loads of its next pair fly while it
-// updates the current one.  Slots are private to a thread: no block barrier
-// between pairs.
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ void cp_async(void *dst, const void *src, int bytes, bool valid) {
-  if (bytes == 8)
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(smem_u32(dst)), "l"(src), "r"(valid ? 8 : 0)
-                 : "memory");
-  else
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(smem_u32(dst)), "l"(src), "r"(valid ? 4 : 0)
-                 : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
-
-// Shared-memory slots of one stage, struct of arrays over the CTA's threads.
-template <bool MASK>
-struct PairStage {
-  float2 v[18][kPB];  // own x y z, other colour same row x y z, rows y+ y- z+ z- (x y z each)
-  float ex[3][kPB];   // the extra other-colour site (x y z)
-  uint32_t pw[MASK ? 7 : 1][kPB];  // point-type words: own, other row, 4 rows, extra
-};
-
-// Where a thread's pair lives and who its neighbours are.
-struct PairGeom {
-  int row, h0, j, k, s, off, exh, offp;
-  bool valid, hasB;
-  float exe, er[4];
-  int rr[4];
-};
-
-__device__ __forceinline__ void pair_geom(const RepDev &R, int c, int t, PairGeom &g) {
-  g.valid = t < R.npair;
-  const int tt = g.valid ? t : 0;
-  g.row = (int)fastdiv((uint32_t)tt, R.hp_m, R.hp_p);
-  g.h0 = 2 * (tt - g.row * R.hp);
-  g.k = (int)fastdiv((uint32_t)g.row, R.ny_m, R.ny_p);
-  g.j = g.row - g.k * R.ny;
-  g.s = (c + g.j + g.k) & 1;
-  g.hasB = g.h0 + 1 < R.hx;
-  g.off = g.row * R.hs + g.h0;
-  g.offp = g.row * R.hps + g.h0;
-  g.exe = 1.f;
-  if (g.s == 0) {
-    g.exh = g.h0 - 1;
-    if (g.exh < 0) { if (R.xb == BOUND_PERIODIC) g.exh = R.hx - 1; else { g.exe = 0.f; g.exh = g.h0; } }
-  } else {
-    g.exh = g.hasB ? g.h0 + 2 : g.h0 + 1;
-    if (g.exh == R.hx) { if (R.xb == BOUND_PERIODIC) g.exh = 0; else { g.exe = 0.f; g.exh = g.h0; } }
-  }
-  const int ny = R.ny, nz = R.nz;
-  g.rr[0] = g.row + 1; g.rr[1] = g.row - 1; g.rr[2] = g.row + ny; g.rr[3] = g.row - ny;
-  g.er[0] = g.er[1] = g.er[2] = g.er[3] = 1.f;
-  if (g.j + 1 == ny) { if (R.yb == BOUND_PERIODIC) g.rr[0] -= ny; else { g.er[0] = 0.f; g.rr[0] = g.row; } }
-  if (g.j == 0) { if (R.yb == BOUND_PERIODIC) g.rr[1] += ny; else { g.er[1] = 0.f; g.rr[1] = g.row; } }
-  if (g.k + 1 == nz) { if (R.zb == BOUND_PERIODIC) g.rr[2] -= ny * nz; else { g.er[2] = 0.f; g.rr[2] = g.row; } }
-  if (g.k == 0) { if (R.zb == BOUND_PERIODIC) g.rr[3] += ny * nz; else { g.er[3] = 0.f; g.rr[3] = g.row; } }
-}
-
-template <bool MASK>
-__device__ __forceinline__ void prefetch_pair(const PassArgs &a, int c, int2 m, PairStage<MASK> &st) {
-  const RepDev &R = a.reps[m.x];
-  PairGeom g;
-  pair_geom(R, c, m.y + (int)threadIdx.x, g);
-  const int P = R.plane, tid = threadIdx.x;
-  const float *Ac = a.dir + R.dir_off + (long long)(c * 3) * P;
-  const float *Oc = a.dir + R.dir_off + (long long)((c ^ 1) * 3) * P;
-  const bool v = g.valid;
-#pragma unroll
-  for (int q = 0; q < 3; q++) {
-    cp_async(&st.v[q][tid], Ac + (long long)q * P + g.off, 8, v);
-    cp_async(&st.v[3 + q][tid], Oc + (long long)q * P + g.off, 8, v);
-    cp_async(&st.ex[q][tid], Oc + (long long)q * P + (long long)g.row * R.hs + g.exh, 4, v && g.exe != 0.f);
-#pragma unroll
-    for (int d = 0; d < 4; d++)
-      cp_async(&st.v[6 + 3 * d + q][tid], Oc + (long long)q * P + (long long)g.rr[d] * R.hs + g.h0, 8,
-               v && g.er[d] != 0.f);
-  }
-  if (MASK) {
-    // 4-byte words holding the needed point-type bytes (rows are 16-byte aligned)
-    const uint8_t *pa = a.pt + R.pt_off + (long long)c * R.pplane;
-    const uint8_t *po = a.pt + R.pt_off + (long long)(c ^ 1) * R.pplane;
-    cp_async(&st.pw[0][tid], pa + (g.offp & ~3), 4, v);
-    cp_async(&st.pw[1][tid], po + (g.offp & ~3), 4, v);
-#pragma unroll
-    for (int d = 0; d < 4; d++) cp_async(&st.pw[2 + d][tid], po + ((g.rr[d] * R.hps + g.h0) & ~3), 4, v && g.er[d] != 0.f);
-    cp_async(&st.pw[6][tid], po + ((g.row * R.hps + g.exh) & ~3), 4, v && g.exe != 0.f);
-  }
-}
-
-__device__ __forceinline__ uchar2 word_pair(uint32_t w, int byte) {
-  const uint32_t x = w >> (8 * byte);
-  return make_uchar2((uint8_t)(x & 0xFF), (uint8_t)((x >> 8) & 0xFF));
-}
-
-template <int POT, bool MASK, bool FIELD, int MODE>
-__device__ __forceinline__ void compute_pair(const PassArgs &a, int c, int2 m, const PairStage<MASK> &st, unsigned &acc,
-                                             float qs[kQ]) {
-  constexpr bool UPD = MODE != MODE_MEASURE_ONLY;
-  const RepDev &R = a.reps[m.x];
-  RepState *S = a.st + m.x;
-  PairGeom g;
-  pair_geom(R, c, m.y + (int)threadIdx.x, g);
-  if (!g.valid) return;
-  const int tid = threadIdx.x, P = R.plane;
-  float2 ax = st.v[0][tid], ay = st.v[1][tid], az = st.v[2][tid];
-  const float2 ox = st.v[3][tid], oy = st.v[4][tid], oz = st.v[5][tid];
-  const float ex = st.ex[0][tid], ey = st.ex[1][tid], ez = st.ex[2][tid];
-  uchar2 pself2 = make_uchar2(1, 1), po2 = make_uchar2(1, 1), pr[4];
-  uint8_t pex = 1;
-  if (MASK) {
-    const int b = g.offp & 3;
-    pself2 = word_pair(st.pw[0][tid], b);
-    po2 = word_pair(st.pw[1][tid], b);
-#pragma unroll
-    for (int d = 0; d < 4; d++) pr[d] = word_pair(st.pw[2 + d][tid], (g.rr[d] * R.hps + g.h0) & 3);
-    pex = (uint8_t)((st.pw[6][tid] >> (8 * ((g.row * R.hps + g.exh) & 3))) & 0xFF);
-  }
-  float uA[3] = {0.f, 0.f, 0.f}, uB[3] = {0.f, 0.f, 0.f};
-  float ang = 0.f, invT = 0.f;
-  if (UPD) {
-    const unsigned long long sw = S->sweep;
-    const uint32_t pid = (uint32_t)(m.y + tid);
-    const uint4 rw = philox4x32_10(make_uint4(pid, (uint32_t)sw, (uint32_t)(sw >> 32), TAG_PLAIN | (uint32_t)c),
-                                   R.seed, R.stream);
-    pair_uniforms(rw, uA, uB);
-    ang = S->ang_var;
-    invT = 1.0f / S->T;
-  }
-  auto wt = [&](float ee, uint8_t pp) { return MASK ? (ee != 0.f && pp != 0 ? 1.f : 0.f) : ee; };
-  float nb[6][3], w[6], e[6];
-  {
-    if (g.s == 0) {
-      nb[0][0] = ox.x; nb[0][1] = oy.x; nb[0][2] = oz.x; e[0] = 1.f; w[0] = wt(1.f, po2.x);
-      nb[1][0] = ex; nb[1][1] = ey; nb[1][2] = ez; e[1] = g.exe; w[1] = wt(g.exe, pex);
-    } else {
-      if (g.hasB) {
-        nb[0][0] = ox.y; nb[0][1] = oy.y; nb[0][2] = oz.y; e[0] = 1.f; w[0] = wt(1.f, po2.y);
-      } else {
-        nb[0][0] = ex; nb[0][1] = ey; nb[0][2] = ez; e[0] = g.exe; w[0] = wt(g.exe, pex);
-      }
-      nb[1][0] = ox.x; nb[1][1] = oy.x; nb[1][2] = oz.x; e[1] = 1.f; w[1] = wt(1.f, po2.x);
-    }
-#pragma unroll
-    for (int d = 0; d < 4; d++) {
-      const float2 X = st.v[6 + 3 * d][tid], Y = st.v[7 + 3 * d][tid], Z = st.v[8 + 3 * d][tid];
-      nb[2 + d][0] = X.x; nb[2 + d][1] = Y.x; nb[2 + d][2] = Z.x;
-      e[2 + d] = g.er[d];
-      w[2 + d] = wt(g.er[d], MASK ? pr[d].x : 1);
-    }
-    const int ps = MASK ? pself2.x : 1;
-    float sx = 0.f, sy = 0.f, sz = 0.f;
-    if (MASK && ps > 1) {
-      const float *nsb = a.ns + R.ns_off + (long long)(c * 3) * P + g.off;
-      sx = __ldg(nsb);
-      sy = __ldg(nsb + P);
-      sz = __ldg(nsb + 2 * P);
-    }
-    const uint32_t nat = (uint32_t)(2 * g.h0 + g.s) + (uint32_t)R.nx * (uint32_t)g.row;
-    acc += site_update<POT, MASK, FIELD, MODE>(R, a, c, ax.x, ay.x, az.x, nb, w, e, ps, sx, sy, sz, uA, ang, invT,
-                                               nat, qs);
-  }
-  if (g.hasB) {
-    if (g.s == 0) {
-      nb[0][0] = ox.y; nb[0][1] = oy.y; nb[0][2] = oz.y; e[0] = 1.f; w[0] = wt(1.f, po2.y);
-      nb[1][0] = ox.x; nb[1][1] = oy.x; nb[1][2] = oz.x; e[1] = 1.f; w[1] = wt(1.f, po2.x);
-    } else {
-      nb[0][0] = ex; nb[0][1] = ey; nb[0][2] = ez; e[0] = g.exe; w[0] = wt(g.exe, pex);
-      nb[1][0] = ox.y; nb[1][1] = oy.y; nb[1][2] = oz.y; e[1] = 1.f; w[1] = wt(1.f, po2.y);
-    }
-#pragma unroll
-    for (int d = 0; d < 4; d++) {
-      const float2 X = st.v[6 + 3 * d][tid], Y = st.v[7 + 3 * d][tid], Z = st.v[8 + 3 * d][tid];
-      nb[2 + d][0] = X.y; nb[2 + d][1] = Y.y; nb[2 + d][2] = Z.y;
-      e[2 + d] = g.er[d];
-      w[2 + d] = wt(g.er[d], MASK ? pr[d].y : 1);
-    }
-    const int ps = MASK ? pself2.y : 1;
-    float sx = 0.f, sy = 0.f, sz = 0.f;
-    if (MASK && ps > 1) {
-      const float *nsb = a.ns + R.ns_off + (long long)(c * 3) * P + g.off + 1;
-      sx = __ldg(nsb);
-      sy = __ldg(nsb + P);
-      sz = __ldg(nsb + 2 * P);
-    }
-    const uint32_t nat = (uint32_t)(2 * g.h0 + 2 + g.s) + (uint32_t)R.nx * (uint32_t)g.row;
-    acc += site_update<POT, MASK, FIELD, MODE>(R, a, c, ax.y, ay.y, az.y, nb, w, e, ps, sx, sy, sz, uB, ang, invT,
-                                               nat, qs);
-  }
-  if (UPD) {
-    float *gA = a.dir + R.dir_off + (long long)(c * 3) * P + g.off;
-    *reinterpret_cast<float2 *>(gA) = ax;
-    *reinterpret_cast<float2 *>(gA + P) = ay;
-    *reinterpret_cast<float2 *>(gA + 2 * P) = az;
-  }
-}
-
-template <int POT, bool MASK, bool FIELD, int MODE>
-__global__ void __launch_bounds__(kPB, MCX_PASS_MIN_BLOCKS) k_pass(PassArgs a) {
-  __shared__ PairStage<MASK> stages[2];
-  const int c = a.colour;
-  const int G = gridDim.x, n = a.nmap;
-  int e = blockIdx.x;
-  if (e < n) prefetch_pair<MASK>(a, c, a.map[e], stages[0]);
-  cp_async_commit();
-  int cur = -1, units = 0;
-  unsigned acc = 0;
-  float qs[kQ];
-#pragma unroll
-  for (int q = 0; q < kQ; q++) qs[q] = 0.f;
-  for (int it = 0; e < n; it++, e += G) {
-    const int2 m = a.map[e];
-    if (e + G < n) prefetch_pair<MASK>(a, c, a.map[e + G], stages[(it + 1) & 1]);
-    cp_async_commit();
-    if (m.x != cur) {
-      if (cur >= 0) {
-        flush_replica<kPB, MODE>(a, cur, units, (unsigned)a.reps[cur].ncta, acc, qs, MASK);
-        acc = 0;
-#pragma unroll
-        for (int q = 0; q < kQ; q++) qs[q] = 0.f;
-      }
-      cur = m.x;
-      units = 0;
-    }
-    cp_async_wait1();
-    compute_pair<POT, MASK, FIELD, MODE>(a, c, m, stages[it & 1], acc, qs);
-    units++;
-  }
-  asm volatile("cp.async.wait_all;" ::: "memory");
-  if (cur >= 0) flush_replica<kPB, MODE>(a, cur, units, (unsigned)a.reps[cur].ncta, acc, qs, MASK);
-}
 
 // ---------------------------------------------------------------------------
 // Staged pass: tiles of rows brought into shared memory by TMA bulk copies.
@@ -1147,10 +668,10 @@ __global__ void k_init(RepDev R, const uint8_t *__restrict__ pt, float *__restri
 template <int POT, bool MASK, bool FIELD>
 static void launch_pass_pmf(int mode, const PassArgs &a, int nblocks, cudaStream_t st) {
   switch (mode) {
-    case MODE_SWEEP: k_pass<POT, MASK, FIELD, MODE_SWEEP><<<nblocks, kPB, 0, st>>>(a); break;
-    case MODE_SWEEP_MEASURE: k_pass<POT, MASK, FIELD, MODE_SWEEP_MEASURE><<<nblocks, kPB, 0, st>>>(a); break;
-    case MODE_MEASURE_ONLY: k_pass<POT, MASK, FIELD, MODE_MEASURE_ONLY><<<nblocks, kPB, 0, st>>>(a); break;
-    default: k_pass<POT, MASK, FIELD, MODE_TRACE><<<nblocks, kPB, 0, st>>>(a); break;
+    case MODE_SWEEP: k_pass<POT, MASK, FIELD, MODE_SWEEP, false><<<nblocks, kPB, 0, st>>>(a); break;
+    case MODE_SWEEP_MEASURE: k_pass<POT, MASK, FIELD, MODE_SWEEP_MEASURE, false><<<nblocks, kPB, 0, st>>>(a); break;
+    case MODE_MEASURE_ONLY: k_pass<POT, MASK, FIELD, MODE_MEASURE_ONLY, false><<<nblocks, kPB, 0, st>>>(a); break;
+    default: k_pass<POT, MASK, FIELD, MODE_TRACE, false><<<nblocks, kPB, 0, st>>>(a); break;
   }
 }
 
@@ -1168,10 +689,10 @@ static void launch_pass_p(const Variant &v, int mode, const PassArgs &a, int nbl
 template <int POT, bool MASK, bool FIELD>
 static const void *pass_fn(int mode) {
   switch (mode) {
-    case MODE_SWEEP: return (const void *)k_pass<POT, MASK, FIELD, MODE_SWEEP>;
-    case MODE_SWEEP_MEASURE: return (const void *)k_pass<POT, MASK, FIELD, MODE_SWEEP_MEASURE>;
-    case MODE_MEASURE_ONLY: return (const void *)k_pass<POT, MASK, FIELD, MODE_MEASURE_ONLY>;
-    default: return (const void *)k_pass<POT, MASK, FIELD, MODE_TRACE>;
+    case MODE_SWEEP: return (const void *)k_pass<POT, MASK, FIELD, MODE_SWEEP, false>;
+    case MODE_SWEEP_MEASURE: return (const void *)k_pass<POT, MASK, FIELD, MODE_SWEEP_MEASURE, false>;
+    case MODE_MEASURE_ONLY: return (const void *)k_pass<POT, MASK, FIELD, MODE_MEASURE_ONLY, false>;
+    default: return (const void *)k_pass<POT, MASK, FIELD, MODE_TRACE, false>;
   }
 }
 

@@ -42,6 +42,9 @@ struct PassArgs {
   float *tr_dE;
   uint8_t *tr_acc;
   float *tr_prop;
+  float *tr_y;  // learned proposal: the network's 4 outputs per site (may be null)
+  // learned proposal: the network's weights in the mcx_mlp.cuh layout
+  const uint8_t *mlp;
   // staged pass: the flat tile list and the shared-memory stage size
   const int4 *tiles;  // (replica, j0, k0, 0)
   int ntiles;
@@ -63,6 +66,12 @@ struct FlushArgs {
 // The direct pass over a.map with `nblocks` persistent CTAs.
 void launch_pass(const Variant &v, int mode, const PassArgs &a, int nblocks, cudaStream_t st);
 int pass_blocks_per_sm(const Variant &v, int mode);
+// The direct pass with the learned proposal (mcx_learned.cu).
+void launch_pass_learned(const Variant &v, int mode, const PassArgs &a, int nblocks, cudaStream_t st);
+int pass_learned_blocks_per_sm(const Variant &v, int mode);
+// Packs FP32 weights (the flat layout of mcx_set_mlp) into the device layout.
+void pack_mlp_weights(const float *flat, uint8_t *out);
+int mlp_device_bytes();
 int pass_block_threads();
 // The staged (TMA) pass over a.tiles with `grid` persistent CTAs.
 void launch_tpass(const Variant &v, int mode, const PassArgs &a, int grid, cudaStream_t st);

@@ -29,6 +29,8 @@ GEOMETRIES = {"bulk": 0, "slab": 1, "sphere": 2, "custom": 3}
 BOUNDS = {"free": 0, "periodic": 1}
 ANCHORINGS = {"homeotropic": 0, "fg": 1, "rp": 2, "strong": 3, "homeotropic_ghrl": 4, "fg_ghrl": 5, "rp_ghrl": 6,
               "strong_ghrl": 7}
+PROPOSALS = {"plain": 0, "vmf_mlp": 1}
+MLP_PARAMS = 6792
 STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "out of memory", 4: "unsupported", 5: "I/O error",
           6: "parse error"}
 
@@ -132,6 +134,11 @@ def lib() -> C.CDLL:
         L.mcx_stream.argtypes = [V]
         L.mcx_stream.restype = V
         L.mcx_pass_timing.argtypes = [V, I, C.POINTER(F), C.POINTER(F)]
+        L.mcx_set_mlp.argtypes = [V, V, I]
+        L.mcx_get_mlp.argtypes = [V, V]
+        L.mcx_set_proposal.argtypes = [V, I]
+        L.mcx_debug_pass_mlp.argtypes = [V, I, I, V, V, V, V]
+        L.mcx_mlp_params.restype = I
         _lib = L
     return _lib
 
@@ -263,6 +270,27 @@ class Engine:
         prop = np.zeros((n, 3), np.float32)
         self._ck(self._L.mcx_debug_pass(self._h, r, colour, _p(dE), _p(acc), _p(prop)))
         return dE, acc, prop
+
+    def set_mlp(self, weights: np.ndarray):
+        w = np.ascontiguousarray(weights, np.float32).reshape(-1)
+        self._ck(self._L.mcx_set_mlp(self._h, _p(w), int(w.size)))
+
+    def get_mlp(self) -> np.ndarray:
+        w = np.zeros(MLP_PARAMS, np.float32)
+        self._ck(self._L.mcx_get_mlp(self._h, _p(w)))
+        return w
+
+    def set_proposal(self, kind: str):
+        self._ck(self._L.mcx_set_proposal(self._h, PROPOSALS[kind]))
+
+    def debug_pass_mlp(self, r: int, colour: int):
+        n = self.sites(r)
+        dE = np.zeros(n, np.float32)
+        acc = np.zeros(n, np.uint8)
+        prop = np.zeros((n, 3), np.float32)
+        y = np.zeros((n, 4), np.float32)
+        self._ck(self._L.mcx_debug_pass_mlp(self._h, r, colour, _p(dE), _p(acc), _p(prop), _p(y)))
+        return dE, acc, prop, y
 
     @property
     def staged(self) -> bool:

@@ -1,0 +1,142 @@
+"""The learned proposal on the GPU against its FP64 reference (oracle/mlp.py).
+
+Per red/black pass, for every updated site: the network's outputs match the
+FP64 forward pass with the engine's BF16 roundings (within 3e-2, set by BF16
+activations and the hardware tanh); the proposal matches the FP64 inverse-CDF
+draw from those outputs and the same Philox uniforms; the accept/reject
+decision matches the FP64 Metropolis-Hastings ratio evaluated on the GPU's
+proposal, except inside the 1e-5 tie band; the state is what the decisions
+say.  And the MH correction is exact: with any weights the learned chain
+samples the same equilibrium E and S as the plain one."""
+import numpy as np
+import pytest
+
+import mcx
+from oracle import mlp as M
+from oracle import oracle as O
+from helpers import desc_from_model, random_state
+
+pytestmark = pytest.mark.gpu
+
+CASES = {
+    "bulk_ll": O.Model(nx=16, ny=8, nz=8, potential="ll"),
+    "slab_ghrl_field": O.Model(nx=12, ny=8, nz=6, geometry="slab", potential="ghrl", k11=1.0, k22=0.6, k33=1.4,
+                               p0=20, elecA=0.4, elecZ=1.0, elecE=1.5,
+                               surfaces=[O.Surface("fg", 2.0), O.Surface("homeotropic", 3.0)]),
+    "sphere_ll": O.Model(nx=12, ny=12, nz=12, geometry="sphere", potential="ll", surfaces=[O.Surface("fg", 1.0)]),
+}
+
+
+def _weights(seed, scale=1.5):
+    rng = np.random.default_rng(seed)
+    params = M.init_params(rng, scale=scale)
+    params[5] = np.array([0.0, 0.0, 0.3, 1.0])  # a typical kappa ~ e
+    return params
+
+
+def _vmf_uniforms(site, seed, stream, sweep):
+    r = O.philox([site, sweep & 0xFFFFFFFF, sweep >> 32, 2], [seed, stream])
+    return O.u24(r)
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_learned_pass_parity(name):
+    m = CASES[name]
+    T, seed, stream = 0.9, 31, 4
+    params = _weights(1)
+    lat = O.Lattice(m)
+    rng = np.random.default_rng(8)
+    ni0 = random_state(m, lat.pt, rng)
+    with mcx.Engine([desc_from_model(m, T=T, seed=seed, stream=stream)]) as eng:
+        eng.set_state(0, ni0)
+        eng.set_mlp(M.pack_weights(params))
+        eng.set_proposal("vmf_mlp")
+        i = np.arange(m.n) % m.nx
+        j = (np.arange(m.n) // m.nx) % m.ny
+        k = np.arange(m.n) // (m.nx * m.ny)
+        ties = 0
+        for colour in (0, 1):
+            before = eng.get_state(0)
+            dE, acc, prop, y = eng.debug_pass_mlp(0, colour)
+            after = eng.get_state(0)
+            upd = (((i + j + k) & 1) == colour) & (lat.pt != 0)
+            assert np.all(acc[~upd] == 255)
+            lat.ni[:] = before
+            sites = np.nonzero(upd)[0]
+            # network outputs
+            nbrs = np.zeros((len(sites), 6, 3))
+            for q, s in enumerate(sites):
+                nbrs[q] = _neighbours(lat, m, int(s))
+            X = M.features(nbrs, T)
+            Yref = M.forward_bf16(params, X)
+            assert np.max(np.abs(y[sites] - Yref)) < 3e-2
+            for q, s in enumerate(sites):
+                u = _vmf_uniforms(int(s), seed, stream, 0)
+                Yg = y[s:s + 1].astype(np.float64)
+                v = M.sample(Yg, u[0:1], u[1:2], u[2:3])[0]
+                assert np.max(np.abs(prop[s] - v)) < 1e-4, (s, prop[s], v)
+                e1, a1 = lat.local_energy_abs(int(s), prop[s])
+                e0, a0 = lat.local_energy_abs(int(s), before[s])
+                assert abs(dE[s] - (e1 - e0)) <= 1e-5 * max(a1 + a0, 1e-3)
+                lr = M.mh_log_ratio(Yg, before[s:s + 1].astype(np.float64), prop[s:s + 1].astype(np.float64),
+                                    np.array([e1 - e0]), T)[0]
+                p = np.exp(min(lr, 50.0))
+                if p < 1 and abs(u[3] - p) <= 1e-5 * (1 + p):
+                    ties += 1
+                    continue
+                assert bool(acc[s]) == (u[3] < p), (s, u[3], p)
+            want = before.copy()
+            want[acc == 1] = prop[acc == 1]
+            assert np.array_equal(after, want)
+
+
+def _neighbours(lat, m, s):
+    """The six neighbour directors of site s in slot order, zero when the bond
+    is absent or the neighbour inactive."""
+    i, j, k = s % m.nx, (s // m.nx) % m.ny, s // (m.nx * m.ny)
+    xb, yb, zb = m.effective_bounds()
+    N = [m.nx, m.ny, m.nz]
+    B = [xb, yb, zb]
+    out = np.zeros((6, 3))
+    for d in range(6):
+        c = [i, j, k]
+        ax = d >> 1
+        c[ax] += -1 if d & 1 else 1
+        if c[ax] < 0 or c[ax] >= N[ax]:
+            if B[ax] != "periodic":
+                continue
+            c[ax] %= N[ax]
+        t = c[0] + m.nx * (c[1] + m.ny * c[2])
+        if lat.pt[t] == 0:
+            continue
+        out[d] = lat.ni[t]
+    return out
+
+
+@pytest.mark.parametrize("T", [0.8, 1.6])
+def test_learned_chain_samples_the_same_equilibrium(T):
+    """Random (untrained) weights: a poor proposal, but the exact MH ratio
+    keeps the Boltzmann distribution -- E and S agree with the plain chain
+    within 4 combined standard errors over 16 replicas each."""
+    m = O.Model(nx=8, ny=8, nz=8, potential="ll")
+    params = _weights(2, scale=1.0)
+    R = 16
+    res = {}
+    for kind in ("plain", "vmf_mlp"):
+        descs = [desc_from_model(m, T=T, seed=100 + r, stream=r) for r in range(R)]
+        with mcx.Engine(descs) as eng:
+            for r in range(R):
+                eng.init_random(r, 7 + r)
+            if kind == "vmf_mlp":
+                eng.set_mlp(M.pack_weights(params))
+                eng.set_proposal("vmf_mlp")
+            eng.sweep(600)
+            eng.reset_stats()
+            eng.sweep(600, measure=True)
+            st = np.array([eng.stats(r) for r in range(R)])
+        n = st[:, mcx.ST_N]
+        res[kind] = (st[:, mcx.ST_E1] / n, st[:, mcx.ST_S1] / n)
+    for q in range(2):
+        a, b = res["plain"][q], res["vmf_mlp"][q]
+        se = np.sqrt(a.var(ddof=1) / len(a) + b.var(ddof=1) / len(b))
+        assert abs(a.mean() - b.mean()) < 4 * se + 1e-4, (q, a.mean(), b.mean(), se)
