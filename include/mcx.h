@@ -171,6 +171,11 @@ mcx_status mcx_get_mask(mcx_engine *eng, int replica, int *pt, float *ns_aos);
 mcx_status mcx_set_temperature(mcx_engine *eng, int replica, float T);
 mcx_status mcx_set_field(mcx_engine *eng, int replica, float elecE);
 mcx_status mcx_set_step(mcx_engine *eng, int replica, float ang_var);
+/* on = 0 freezes the step size (the reference adapts it after every sweep
+ * towards 50% acceptance, src/evolve.cpp:169-178; a frozen step keeps the
+ * chain time-homogeneous for autocorrelation measurements); 1 restores the
+ * reference's rule (the default).  No counterpart in the reference. */
+mcx_status mcx_set_adapt(mcx_engine *eng, int replica, int on);
 
 /* n_sweeps red/black Metropolis sweeps of every replica, on the engine's
  * stream (asynchronous).  measure != 0 measures E, Q and S after every sweep
@@ -231,6 +236,47 @@ mcx_status mcx_set_proposal(mcx_engine *eng, int kind);
  * mlp_out may be NULL). */
 mcx_status mcx_debug_pass_mlp(mcx_engine *eng, int replica, int colour, float *dE, unsigned char *acc,
                               float *proposal_aos, float *mlp_out);
+
+/* Training of the learned proposal on the GPU (no counterpart in the
+ * reference).  A training sample is MCX_SAMPLE_FLOATS floats: the 19 network
+ * inputs of one active site, its director (3), then the replica and the
+ * site's natural index (x + nx (y + ny z)) as int32 bit patterns.  The loss is
+ * the mean negative log-density of the directors under the mixture, i.e.
+ * maximum likelihood of the conditional distribution of a site given its
+ * neighbours when the states are in equilibrium.
+ *
+ * mcx_collect_samples draws n sites (uniformly among each replica's active
+ * sites; replicas in turn by blocks of 256 samples) from the current states
+ * and copies the samples to `out` (host, may be NULL to keep them on the
+ * device only).  augment: MCX_AUG_FLIP flips each director's sign at random
+ * (always a symmetry); MCX_AUG_ROTATE applies one uniform random rotation to
+ * all 7 directors of a sample (a symmetry only of field-free Lebwohl-Lasher
+ * replicas without surfaces, rejected otherwise).
+ *
+ * mcx_train_mlp collects cfg->samples samples (as above; 0 reuses the samples
+ * the engine holds: its last collection or mcx_mlp_grad input) and runs cfg->steps
+ * Adam steps (beta1 0.9, beta2 0.999, eps 1e-8) on minibatches of cfg->batch
+ * drawn with replacement, starting from the current weights (mcx_set_mlp
+ * first); the Adam moments persist across calls until mcx_set_mlp.  The
+ * trained weights become the proposal's; loss (steps floats, may be NULL)
+ * receives each step's minibatch loss.
+ *
+ * mcx_mlp_grad evaluates the loss and its gradient (MCX_MLP_PARAMS floats,
+ * the weight layout) at the current weights over n host samples (only the
+ * first 22 floats of each are read), with the training kernel. */
+#define MCX_SAMPLE_FLOATS 24
+enum { MCX_AUG_FLIP = 1, MCX_AUG_ROTATE = 2 };
+typedef struct {
+  int samples;
+  int batch;
+  int steps;
+  float lr;
+  unsigned int seed;
+  int augment;
+} mcx_train_config;
+mcx_status mcx_collect_samples(mcx_engine *eng, int n, unsigned int seed, int augment, float *out);
+mcx_status mcx_train_mlp(mcx_engine *eng, const mcx_train_config *cfg, float *loss);
+mcx_status mcx_mlp_grad(mcx_engine *eng, const float *samples, int n, float *grad, float *loss);
 
 /* The engine's CUDA stream (a cudaStream_t), for callers that record events
  * or order their own work against the engine's. */

@@ -74,7 +74,7 @@ struct RepState {
   unsigned long long meas;   // measured sweeps done: the ring-slot counter
   unsigned int acc[kLanes];  // accepted moves of the sweep in progress, by lane
   unsigned int done;         // CTAs of the running colour-1 pass that finished
-  unsigned int pad;
+  unsigned int frozen;        // nonzero: the step size stays fixed (no adaptation)
 };
 
 // Running sums (doubles), indexed by the MCX_ST_* layout of mcx.h.

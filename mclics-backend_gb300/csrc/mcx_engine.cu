@@ -68,6 +68,15 @@ struct mcx_engine {
   uint8_t *d_mlp = nullptr;
   std::vector<float> mlp;  // FP32 weights as last set or trained
   int lgrid[4] = {0, 0, 0, 0};
+  // training of the network: FP32 master weights, Adam moments, gradient
+  float *d_w = nullptr, *d_am = nullptr, *d_av = nullptr, *d_g = nullptr, *d_loss = nullptr;
+  bool w_stale = true;  // d_w does not hold e->mlp yet (Adam restarts)
+  int adam_step = 0;
+  float *d_samples = nullptr;
+  long long sample_cap = 0;
+  int *d_idx = nullptr, *d_repof = nullptr;
+  long long idx_cap = 0, repof_cap = 0, loss_bytes = 0;
+  int held_samples = 0;  // samples in d_samples (last collection or mcx_mlp_grad upload)
 };
 
 static mcx_status fail(mcx_engine *e, mcx_status st, const char *fmt, ...) {
@@ -171,6 +180,14 @@ static void free_engine(mcx_engine *e) {
   cudaFree(e->d_tiles);
   cudaFree(e->d_err);
   cudaFree(e->d_mlp);
+  cudaFree(e->d_w);
+  cudaFree(e->d_am);
+  cudaFree(e->d_av);
+  cudaFree(e->d_g);
+  cudaFree(e->d_loss);
+  cudaFree(e->d_samples);
+  cudaFree(e->d_idx);
+  cudaFree(e->d_repof);
   if (e->stream) cudaStreamDestroy(e->stream);
   delete e;
 }
@@ -546,6 +563,10 @@ extern "C" mcx_status mcx_set_step(mcx_engine *e, int r, float a) {
   return set_scalar(e, r, offsetof(RepState, ang_var), a, false);
 }
 
+extern "C" mcx_status mcx_set_adapt(mcx_engine *e, int r, int on) {
+  return set_scalar(e, r, offsetof(RepState, frozen), on ? 0u : 1u, false);
+}
+
 static PassArgs pass_args(mcx_engine *e) {
   PassArgs pa{};
   pa.reps = e->d_rep;
@@ -682,11 +703,23 @@ static void drop_graphs(mcx_engine *e) {
 
 extern "C" int mcx_mlp_params(void) { return MCX_MLP_PARAMS; }
 
+static mcx_status upload_mlp(mcx_engine *e, const float *w);
+
 extern "C" mcx_status mcx_set_mlp(mcx_engine *e, const float *w, int n) {
   if (!e) return fail(nullptr, MCX_ERR_INVALID, "null engine");
   if (!w || n != MCX_MLP_PARAMS) return fail(e, MCX_ERR_INVALID, "mcx_set_mlp: expected %d weights, got %d", MCX_MLP_PARAMS, n);
   for (int i = 0; i < n; i++)
     if (!(w[i] == w[i]) || w[i] > 1e30f || w[i] < -1e30f) return fail(e, MCX_ERR_INVALID, "mcx_set_mlp: weight %d is not finite", i);
+  if (mcx_status st = upload_mlp(e, w)) return st;
+  e->mlp.assign(w, w + n);
+  e->w_stale = true;
+  drop_graphs(e);  // captured launches hold the weight pointer only, but keep it simple
+  return MCX_OK;
+}
+
+// Packs FP32 weights into the inference layout on the device (allocating it
+// and sizing the learned pass's grid on first use).
+static mcx_status upload_mlp(mcx_engine *e, const float *w) {
   std::vector<uint8_t> packed(mlp_device_bytes());
   pack_mlp_weights(w, packed.data());
   CK(e, cudaStreamSynchronize(e->stream));
@@ -704,8 +737,6 @@ extern "C" mcx_status mcx_set_mlp(mcx_engine *e, const float *w, int n) {
     }
   }
   CK(e, cudaMemcpy(e->d_mlp, packed.data(), packed.size(), cudaMemcpyHostToDevice));
-  e->mlp.assign(w, w + n);
-  drop_graphs(e);  // captured launches hold the weight pointer only, but keep it simple
   return MCX_OK;
 }
 
@@ -723,6 +754,147 @@ extern "C" mcx_status mcx_set_proposal(mcx_engine *e, int kind) {
   CK(e, cudaStreamSynchronize(e->stream));
   e->proposal = kind;
   drop_graphs(e);
+  return MCX_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Training of the learned proposal (kernels in mcx_train.cu).
+// ---------------------------------------------------------------------------
+static cudaError_t ensure_bytes(void **p, long long *cap, long long bytes) {
+  if (*cap >= bytes) return cudaSuccess;
+  cudaFree(*p);
+  *p = nullptr;
+  *cap = 0;
+  cudaError_t r = cudaMalloc(p, (size_t)bytes);
+  if (r == cudaSuccess) *cap = bytes;
+  return r;
+}
+
+// The FP32 master weights and Adam moments on the device, current with e->mlp.
+static mcx_status train_prepare(mcx_engine *e) {
+  if (e->mlp.empty()) return fail(e, MCX_ERR_INVALID, "set the network weights (mcx_set_mlp) first");
+  const size_t wb = sizeof(float) * MCX_MLP_PARAMS;
+  if (!e->d_w) {
+    float **bufs[4] = {&e->d_w, &e->d_am, &e->d_av, &e->d_g};
+    for (float **b : bufs) {
+      cudaError_t r = cudaMalloc(b, wb);
+      if (r != cudaSuccess) return fail(e, MCX_ERR_NOMEM, "training buffers: %s", cudaGetErrorString(r));
+    }
+  }
+  if (e->w_stale) {
+    CK(e, cudaMemcpyAsync(e->d_w, e->mlp.data(), wb, cudaMemcpyHostToDevice, e->stream));
+    CK(e, cudaMemsetAsync(e->d_am, 0, wb, e->stream));
+    CK(e, cudaMemsetAsync(e->d_av, 0, wb, e->stream));
+    CK(e, cudaStreamSynchronize(e->stream));
+    e->adam_step = 0;
+    e->w_stale = false;
+  }
+  return MCX_OK;
+}
+
+static mcx_status check_augment(mcx_engine *e, int augment) {
+  if (augment & ~(MCX_AUG_FLIP | MCX_AUG_ROTATE)) return fail(e, MCX_ERR_INVALID, "unknown augmentation bits %d", augment);
+  if (augment & MCX_AUG_ROTATE) {
+    bool ok = e->var.pot == POT_LL && !e->var.field;
+    for (const auto &d : e->desc) ok = ok && d.n_surfaces == 0;
+    if (!ok)
+      return fail(e, MCX_ERR_INVALID,
+                  "MCX_AUG_ROTATE needs Lebwohl-Lasher replicas without field or surfaces (a rotation is not a symmetry otherwise)");
+  }
+  return MCX_OK;
+}
+
+// Draws n samples into e->d_samples (queued on the engine stream).
+static mcx_status collect(mcx_engine *e, int n, unsigned seed, int augment) {
+  const int F = sample_floats();
+  CK(e, ensure_bytes((void **)&e->d_samples, &e->sample_cap, (long long)n * F * sizeof(float)));
+  const int nb = (n + 255) / 256;
+  std::vector<int> rep_of(nb);
+  for (int b = 0; b < nb; b++) rep_of[b] = b % e->nrep;
+  CK(e, ensure_bytes((void **)&e->d_repof, &e->repof_cap, (long long)nb * sizeof(int)));
+  CK(e, cudaMemcpyAsync(e->d_repof, rep_of.data(), sizeof(int) * nb, cudaMemcpyHostToDevice, e->stream));
+  CK(e, launch_collect(e->d_rep, e->d_st, e->d_dir, e->d_pt, e->d_samples, e->d_repof, n, seed, augment, e->stream));
+  e->launches++;
+  e->held_samples = n;
+  // rep_of is a local vector: the copy must finish before it goes
+  CK(e, cudaStreamSynchronize(e->stream));
+  return MCX_OK;
+}
+
+static int grad_grid(int n) {
+  int dev = 0, nsm = 148;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  return std::max(1, std::min((n + 63) / 64, 2 * nsm));
+}
+
+extern "C" mcx_status mcx_collect_samples(mcx_engine *e, int n, unsigned int seed, int augment, float *out) {
+  if (!e) return fail(nullptr, MCX_ERR_INVALID, "null engine");
+  if (n < 1) return fail(e, MCX_ERR_INVALID, "mcx_collect_samples: n = %d", n);
+  if (mcx_status st = check_augment(e, augment)) return st;
+  if (mcx_status st = collect(e, n, seed, augment)) return st;
+  if (out) {
+    CK(e, cudaMemcpyAsync(out, e->d_samples, sizeof(float) * (size_t)n * sample_floats(), cudaMemcpyDeviceToHost, e->stream));
+    CK(e, cudaStreamSynchronize(e->stream));
+  }
+  return MCX_OK;
+}
+
+extern "C" mcx_status mcx_mlp_grad(mcx_engine *e, const float *samples, int n, float *grad, float *loss) {
+  if (!e) return fail(nullptr, MCX_ERR_INVALID, "null engine");
+  if (!samples || !grad || n < 1) return fail(e, MCX_ERR_INVALID, "mcx_mlp_grad: bad arguments");
+  if (mcx_status st = train_prepare(e)) return st;
+  const size_t sb = sizeof(float) * (size_t)n * sample_floats();
+  CK(e, ensure_bytes((void **)&e->d_samples, &e->sample_cap, (long long)sb));
+  CK(e, ensure_bytes((void **)&e->d_loss, &e->loss_bytes, sizeof(float)));
+  CK(e, cudaMemcpyAsync(e->d_samples, samples, sb, cudaMemcpyHostToDevice, e->stream));
+  e->held_samples = n;
+  CK(e, cudaMemsetAsync(e->d_g, 0, sizeof(float) * MCX_MLP_PARAMS, e->stream));
+  CK(e, cudaMemsetAsync(e->d_loss, 0, sizeof(float), e->stream));
+  CK(e, launch_mlp_grad(e->d_w, e->d_samples, nullptr, n, e->d_g, e->d_loss, grad_grid(n), e->stream));
+  e->launches++;
+  CK(e, cudaMemcpyAsync(grad, e->d_g, sizeof(float) * MCX_MLP_PARAMS, cudaMemcpyDeviceToHost, e->stream));
+  float l = 0.f;
+  CK(e, cudaMemcpyAsync(&l, e->d_loss, sizeof(float), cudaMemcpyDeviceToHost, e->stream));
+  CK(e, cudaStreamSynchronize(e->stream));
+  if (loss) *loss = l;
+  return MCX_OK;
+}
+
+extern "C" mcx_status mcx_train_mlp(mcx_engine *e, const mcx_train_config *cfg, float *loss) {
+  if (!e) return fail(nullptr, MCX_ERR_INVALID, "null engine");
+  if (!cfg) return fail(e, MCX_ERR_INVALID, "mcx_train_mlp: null config");
+  if (cfg->samples < 0 || cfg->batch < 1 || cfg->steps < 0)
+    return fail(e, MCX_ERR_INVALID, "mcx_train_mlp: samples %d, batch %d, steps %d", cfg->samples, cfg->batch, cfg->steps);
+  if (cfg->samples == 0 && e->held_samples == 0)
+    return fail(e, MCX_ERR_INVALID, "mcx_train_mlp: samples = 0 reuses the last collection, but there is none");
+  if (!(cfg->lr > 0.f) || cfg->lr > 1.f) return fail(e, MCX_ERR_INVALID, "mcx_train_mlp: learning rate %g", (double)cfg->lr);
+  if (mcx_status st = check_augment(e, cfg->augment)) return st;
+  if (mcx_status st = train_prepare(e)) return st;
+  if (cfg->samples > 0)
+    if (mcx_status st = collect(e, cfg->samples, cfg->seed, cfg->augment)) return st;
+  const int nsamp = e->held_samples;
+  CK(e, ensure_bytes((void **)&e->d_idx, &e->idx_cap, (long long)cfg->batch * sizeof(int)));
+  CK(e, ensure_bytes((void **)&e->d_loss, &e->loss_bytes, (long long)std::max(1, cfg->steps) * sizeof(float)));
+  CK(e, cudaMemsetAsync(e->d_loss, 0, sizeof(float) * std::max(1, cfg->steps), e->stream));
+  const int grid = grad_grid(cfg->batch);
+  for (int s = 0; s < cfg->steps; s++) {
+    e->adam_step++;
+    CK(e, launch_batch_index(e->d_idx, cfg->batch, nsamp, cfg->seed, (uint32_t)e->adam_step, e->stream));
+    CK(e, cudaMemsetAsync(e->d_g, 0, sizeof(float) * MCX_MLP_PARAMS, e->stream));
+    CK(e, launch_mlp_grad(e->d_w, e->d_samples, e->d_idx, cfg->batch, e->d_g, e->d_loss + s, grid, e->stream));
+    CK(e, launch_adam(e->d_w, e->d_am, e->d_av, e->d_g, e->adam_step, cfg->lr, e->stream));
+    e->launches += 3;
+  }
+  std::vector<float> w(MCX_MLP_PARAMS);
+  CK(e, cudaMemcpyAsync(w.data(), e->d_w, sizeof(float) * MCX_MLP_PARAMS, cudaMemcpyDeviceToHost, e->stream));
+  if (loss && cfg->steps > 0)
+    CK(e, cudaMemcpyAsync(loss, e->d_loss, sizeof(float) * cfg->steps, cudaMemcpyDeviceToHost, e->stream));
+  CK(e, cudaStreamSynchronize(e->stream));
+  for (int i = 0; i < MCX_MLP_PARAMS; i++)
+    if (!(w[i] == w[i])) return fail(e, MCX_ERR_CUDA, "mcx_train_mlp: weight %d diverged (NaN); lower the learning rate", i);
+  if (mcx_status st = upload_mlp(e, w.data())) return st;
+  e->mlp = w;
   return MCX_OK;
 }
 

@@ -90,4 +90,14 @@ void launch_split_to_mask(const RepDev &R, const uint8_t *pt, const float *ns, i
 void launch_init(const RepDev &R, const uint8_t *pt, float *dir, int mode, uint32_t seed, float fx, float fy, float fz,
                  cudaStream_t st);
 
+// Training of the learned proposal's network (mcx_train.cu).
+int train_smem_bytes();
+int sample_floats();
+cudaError_t launch_collect(const RepDev *reps, const RepState *st, const float *dir, const uint8_t *pt, float *out,
+                           const int *rep_of, int n, uint32_t seed, int augment, cudaStream_t s);
+cudaError_t launch_mlp_grad(const float *w, const float *samples, const int *index, int n, float *grad, float *loss,
+                            int grid, cudaStream_t s);
+cudaError_t launch_adam(float *w, float *m, float *v, const float *g, int step, float lr, cudaStream_t s);
+cudaError_t launch_batch_index(int *idx, int n, int nsamples, uint32_t seed, uint32_t step, cudaStream_t s);
+
 }  // namespace mcx

@@ -248,7 +248,8 @@ __device__ __forceinline__ void flush_replica(const PassArgs &a, int r, int unit
       // src/evolve.cpp:169-178 with the reference's float/double rounding
       float av = S->ang_var;
       const double ratio = 1.0 * (double)tot / (double)R.valid;
-      if (ratio < 0.5) {
+      if (S->frozen) {
+      } else if (ratio < 0.5) {
         av = (float)((double)av * 0.99);
         if ((double)av < 0.01) av = (float)0.01;
       } else if (ratio > 0.5) {

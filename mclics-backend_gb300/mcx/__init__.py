@@ -31,6 +31,8 @@ ANCHORINGS = {"homeotropic": 0, "fg": 1, "rp": 2, "strong": 3, "homeotropic_ghrl
               "strong_ghrl": 7}
 PROPOSALS = {"plain": 0, "vmf_mlp": 1}
 MLP_PARAMS = 6792
+SAMPLE_FLOATS = 24
+AUG_FLIP, AUG_ROTATE = 1, 2
 STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "out of memory", 4: "unsupported", 5: "I/O error",
           6: "parse error"}
 
@@ -65,6 +67,12 @@ class ReplicaDesc(C.Structure):
         ("phi_s", C.c_float * MAX_SURFACES),
         ("radius", C.c_float),
     ]
+
+
+class TrainConfig(C.Structure):
+    """mcx_train_config of include/mcx.h."""
+    _fields_ = [("samples", C.c_int), ("batch", C.c_int), ("steps", C.c_int), ("lr", C.c_float),
+                ("seed", C.c_uint), ("augment", C.c_int)]
 
 
 def replica(nx=16, ny=16, nz=16, geometry="bulk", xbound="periodic", ybound="periodic", zbound="periodic",
@@ -118,6 +126,7 @@ def lib() -> C.CDLL:
         L.mcx_set_temperature.argtypes = [V, I, F]
         L.mcx_set_field.argtypes = [V, I, F]
         L.mcx_set_step.argtypes = [V, I, F]
+        L.mcx_set_adapt.argtypes = [V, I, I]
         L.mcx_sweep.argtypes = [V, I, I]
         L.mcx_sync.argtypes = [V]
         L.mcx_measure.argtypes = [V, I, V]
@@ -139,6 +148,9 @@ def lib() -> C.CDLL:
         L.mcx_set_proposal.argtypes = [V, I]
         L.mcx_debug_pass_mlp.argtypes = [V, I, I, V, V, V, V]
         L.mcx_mlp_params.restype = I
+        L.mcx_collect_samples.argtypes = [V, I, C.c_uint, I, V]
+        L.mcx_train_mlp.argtypes = [V, C.POINTER(TrainConfig), V]
+        L.mcx_mlp_grad.argtypes = [V, V, I, V, V]
         _lib = L
     return _lib
 
@@ -235,6 +247,9 @@ class Engine:
     def set_step(self, ang_var: float, r: int = -1):
         self._ck(self._L.mcx_set_step(self._h, r, ang_var))
 
+    def set_adapt(self, on: bool, r: int = -1):
+        self._ck(self._L.mcx_set_adapt(self._h, r, 1 if on else 0))
+
     def sweep(self, n: int, measure: bool = False):
         self._ck(self._L.mcx_sweep(self._h, n, 1 if measure else 0))
 
@@ -291,6 +306,33 @@ class Engine:
         y = np.zeros((n, 4), np.float32)
         self._ck(self._L.mcx_debug_pass_mlp(self._h, r, colour, _p(dE), _p(acc), _p(prop), _p(y)))
         return dE, acc, prop, y
+
+    def collect_samples(self, n: int, seed: int = 0, augment: int = 0) -> np.ndarray:
+        """n training samples from the current states: [n, 24] float32 (19
+        inputs, the director, then replica and natural site index as int32
+        bit patterns in columns 22, 23)."""
+        out = np.zeros((n, SAMPLE_FLOATS), np.float32)
+        self._ck(self._L.mcx_collect_samples(self._h, int(n), int(seed) & 0xFFFFFFFF, int(augment), _p(out)))
+        return out
+
+    def train_mlp(self, samples: int, batch: int, steps: int, lr: float = 1e-3, seed: int = 0,
+                  augment: int = 0) -> np.ndarray:
+        """Collects `samples` samples and runs `steps` Adam steps on the GPU;
+        returns each step's minibatch loss."""
+        cfg = TrainConfig(int(samples), int(batch), int(steps), float(lr), int(seed) & 0xFFFFFFFF, int(augment))
+        loss = np.zeros(max(1, steps), np.float32)
+        self._ck(self._L.mcx_train_mlp(self._h, C.byref(cfg), _p(loss)))
+        return loss[:steps]
+
+    def mlp_grad(self, samples: np.ndarray):
+        """(loss, gradient) of the mean negative log-likelihood at the current
+        weights over host samples [n, >= 22] (columns 0..21 read)."""
+        s = np.zeros((samples.shape[0], SAMPLE_FLOATS), np.float32)
+        s[:, :22] = samples[:, :22]
+        g = np.zeros(MLP_PARAMS, np.float32)
+        loss = np.zeros(1, np.float32)
+        self._ck(self._L.mcx_mlp_grad(self._h, _p(s), int(s.shape[0]), _p(g), _p(loss)))
+        return float(loss[0]), g
 
     @property
     def staged(self) -> bool:

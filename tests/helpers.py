@@ -18,3 +18,26 @@ def random_state(m: O.Model, pt: np.ndarray, rng) -> np.ndarray:
     ni = O.random_directors(m.n, rng)
     ni[pt == 0] = (0, 0, 1)
     return ni
+
+
+def neighbours(lat, m, s):
+    """The six neighbour directors of site s in slot order, zero when the bond
+    is absent or the neighbour inactive."""
+    i, j, k = s % m.nx, (s // m.nx) % m.ny, s // (m.nx * m.ny)
+    xb, yb, zb = m.effective_bounds()
+    N = [m.nx, m.ny, m.nz]
+    B = [xb, yb, zb]
+    out = np.zeros((6, 3))
+    for d in range(6):
+        c = [i, j, k]
+        ax = d >> 1
+        c[ax] += -1 if d & 1 else 1
+        if c[ax] < 0 or c[ax] >= N[ax]:
+            if B[ax] != "periodic":
+                continue
+            c[ax] %= N[ax]
+        t = c[0] + m.nx * (c[1] + m.ny * c[2])
+        if lat.pt[t] == 0:
+            continue
+        out[d] = lat.ni[t]
+    return out

@@ -14,7 +14,7 @@ import pytest
 import mcx
 from oracle import mlp as M
 from oracle import oracle as O
-from helpers import desc_from_model, random_state
+from helpers import desc_from_model, neighbours, random_state
 
 pytestmark = pytest.mark.gpu
 
@@ -66,7 +66,7 @@ def test_learned_pass_parity(name):
             # network outputs
             nbrs = np.zeros((len(sites), 6, 3))
             for q, s in enumerate(sites):
-                nbrs[q] = _neighbours(lat, m, int(s))
+                nbrs[q] = neighbours(lat, m, int(s))
             X = M.features(nbrs, T)
             Yref = M.forward_bf16(params, X)
             assert np.max(np.abs(y[sites] - Yref)) < 3e-2
@@ -88,29 +88,6 @@ def test_learned_pass_parity(name):
             want = before.copy()
             want[acc == 1] = prop[acc == 1]
             assert np.array_equal(after, want)
-
-
-def _neighbours(lat, m, s):
-    """The six neighbour directors of site s in slot order, zero when the bond
-    is absent or the neighbour inactive."""
-    i, j, k = s % m.nx, (s // m.nx) % m.ny, s // (m.nx * m.ny)
-    xb, yb, zb = m.effective_bounds()
-    N = [m.nx, m.ny, m.nz]
-    B = [xb, yb, zb]
-    out = np.zeros((6, 3))
-    for d in range(6):
-        c = [i, j, k]
-        ax = d >> 1
-        c[ax] += -1 if d & 1 else 1
-        if c[ax] < 0 or c[ax] >= N[ax]:
-            if B[ax] != "periodic":
-                continue
-            c[ax] %= N[ax]
-        t = c[0] + m.nx * (c[1] + m.ny * c[2])
-        if lat.pt[t] == 0:
-            continue
-        out[d] = lat.ni[t]
-    return out
 
 
 @pytest.mark.parametrize("T", [0.8, 1.6])
