@@ -3,7 +3,7 @@
 //
 // Network: 19 inputs (six neighbour directors, T) -> 64 -> 64 -> 4 outputs
 // (mean axis mu, log kappa), GELU (tanh form) between layers, BF16 weights and
-// activations, FP32 accumulation.  One warp evaluates it for 64 sites as four
+// activations, FP32 accumulation; the GELU itself in packed BF16 arithmetic.  One warp evaluates it for 64 sites as four
 // 16-row tiles with mma.sync m16n8k16 (BF16 in, FP32 out); a layer's FP32
 // accumulator fragments become the next layer's BF16 A fragments in
 // registers, so only the inputs and the 4 outputs pass through shared memory.
@@ -58,6 +58,27 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
   return *reinterpret_cast<const uint32_t *>(&v);
 }
 
+// GELU of two FP32 pre-activations, evaluated in packed BF16 arithmetic and
+// returned packed (the next layer's operand).  Each step rounds to BF16:
+//   x = bf16(a), x2 = x*x, t = x2*(c*0.044715) + c, u = x*t,
+//   th = tanh(u) (hardware approximation), h = x*0.5, y = h*th + h
+// with c = sqrt(2/pi) and the constants rounded to BF16; half the
+// instructions and half the SFU operations of the FP32 form.
+__device__ __forceinline__ uint32_t gelu_bf16x2(float a, float b) {
+  const uint32_t kC = 0x3F4C3F4Cu;    // bf16(0.7978845608) = 0.796875, twice
+  const uint32_t kC3 = 0x3D123D12u;   // bf16(0.7978845608 * 0.044715) = 0.03564453125, twice
+  const uint32_t kHalf = 0x3F003F00u; // 0.5, twice
+  const uint32_t x = pack_bf16(a, b);
+  uint32_t x2, t, u, th, h, y;
+  asm("mul.rn.bf16x2 %0, %1, %1;" : "=r"(x2) : "r"(x));
+  asm("fma.rn.bf16x2 %0, %1, %2, %3;" : "=r"(t) : "r"(x2), "r"(kC3), "r"(kC));
+  asm("mul.rn.bf16x2 %0, %1, %2;" : "=r"(u) : "r"(x), "r"(t));
+  asm("tanh.approx.bf16x2 %0, %1;" : "=r"(th) : "r"(u));
+  asm("mul.rn.bf16x2 %0, %1, %2;" : "=r"(h) : "r"(x), "r"(kHalf));
+  asm("fma.rn.bf16x2 %0, %1, %2, %1;" : "=r"(y) : "r"(h), "r"(th));
+  return y;
+}
+
 __device__ __forceinline__ uint32_t lds32(const uint8_t *p) { return *reinterpret_cast<const uint32_t *>(p); }
 
 // The network for 64 rows of X (bf16, row stride kXs) -> Y (64 x 4 floats),
@@ -98,10 +119,10 @@ __device__ __forceinline__ void mlp_warp(const uint8_t *W, const __nv_bfloat16 *
           mma_bf16(h[half], a1[kt], lds32(wr), lds32(wr + 16));
         }
       }
-      a2[q][0] = pack_bf16(gelu(h[0][0]), gelu(h[0][1]));
-      a2[q][1] = pack_bf16(gelu(h[0][2]), gelu(h[0][3]));
-      a2[q][2] = pack_bf16(gelu(h[1][0]), gelu(h[1][1]));
-      a2[q][3] = pack_bf16(gelu(h[1][2]), gelu(h[1][3]));
+      a2[q][0] = gelu_bf16x2(h[0][0], h[0][1]);
+      a2[q][1] = gelu_bf16x2(h[0][2], h[0][3]);
+      a2[q][2] = gelu_bf16x2(h[1][0], h[1][1]);
+      a2[q][3] = gelu_bf16x2(h[1][2], h[1][3]);
     }
     // layer 2 in pairs of n-tiles, each pair feeding one layer-3 k-tile
     float y[4] = {0.f, 0.f, 0.f, 0.f};
@@ -123,10 +144,10 @@ __device__ __forceinline__ void mlp_warp(const uint8_t *W, const __nv_bfloat16 *
         }
       }
       uint32_t a3[4];
-      a3[0] = pack_bf16(gelu(h[0][0]), gelu(h[0][1]));
-      a3[1] = pack_bf16(gelu(h[0][2]), gelu(h[0][3]));
-      a3[2] = pack_bf16(gelu(h[1][0]), gelu(h[1][1]));
-      a3[3] = pack_bf16(gelu(h[1][2]), gelu(h[1][3]));
+      a3[0] = gelu_bf16x2(h[0][0], h[0][1]);
+      a3[1] = gelu_bf16x2(h[0][2], h[0][3]);
+      a3[2] = gelu_bf16x2(h[1][0], h[1][1]);
+      a3[3] = gelu_bf16x2(h[1][2], h[1][3]);
       const uint8_t *wr = W3 + (g * kW3s + q * 16 + 2 * tg) * 2;
       mma_bf16(y, a3, lds32(wr), lds32(wr + 16));
     }

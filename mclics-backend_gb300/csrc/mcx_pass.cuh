@@ -687,9 +687,11 @@ __device__ __forceinline__ void compute_pair_learned(const PassArgs &a, int c, i
 // input rows and 64 output rows.
 constexpr int kLearnSmem = kMlpBytes + (kPB / 32) * (64 * kXs * 2 + 64 * 4 * 4);
 
+// The learned pass is bound by arithmetic, not by loads: it keeps one stage
+// (no prefetch of the next pair) so that three CTAs fit on an SM.
 template <int POT, bool MASK, bool FIELD, int MODE, bool LEARN>
-__global__ void __launch_bounds__(kPB, LEARN ? 2 : MCX_PASS_MIN_BLOCKS) k_pass(PassArgs a) {
-  __shared__ PairStage<MASK> stages[2];
+__global__ void __launch_bounds__(kPB, LEARN ? 3 : MCX_PASS_MIN_BLOCKS) k_pass(PassArgs a) {
+  __shared__ PairStage<MASK> stages[LEARN ? 1 : 2];
   extern __shared__ __align__(16) uint8_t dyn_smem[];
   const int c = a.colour;
   uint8_t *mlpW = dyn_smem;
@@ -703,7 +705,7 @@ __global__ void __launch_bounds__(kPB, LEARN ? 2 : MCX_PASS_MIN_BLOCKS) k_pass(P
   }
   const int G = gridDim.x, n = a.nmap;
   int e = blockIdx.x;
-  if (e < n) prefetch_pair<MASK>(a, c, a.map[e], stages[0]);
+  if (!LEARN && e < n) prefetch_pair<MASK>(a, c, a.map[e], stages[0]);
   cp_async_commit();
   int cur = -1, units = 0;
   unsigned acc = 0;
@@ -712,7 +714,11 @@ __global__ void __launch_bounds__(kPB, LEARN ? 2 : MCX_PASS_MIN_BLOCKS) k_pass(P
   for (int q = 0; q < kQ; q++) qs[q] = 0.f;
   for (int it = 0; e < n; it++, e += G) {
     const int2 m = a.map[e];
-    if (e + G < n) prefetch_pair<MASK>(a, c, a.map[e + G], stages[(it + 1) & 1]);
+    if (LEARN) {
+      prefetch_pair<MASK>(a, c, m, stages[0]);
+    } else if (e + G < n) {
+      prefetch_pair<MASK>(a, c, a.map[e + G], stages[(it + 1) & 1]);
+    }
     cp_async_commit();
     if (m.x != cur) {
       if (cur >= 0) {
@@ -724,11 +730,14 @@ __global__ void __launch_bounds__(kPB, LEARN ? 2 : MCX_PASS_MIN_BLOCKS) k_pass(P
       cur = m.x;
       units = 0;
     }
-    cp_async_wait1();
-    if (LEARN)
-      compute_pair_learned<POT, MASK, FIELD, MODE>(a, c, m, stages[it & 1], mlpW, mlpX, mlpY, acc, qs);
-    else
+    if (LEARN) {
+      asm volatile("cp.async.wait_all;" ::: "memory");
+      compute_pair_learned<POT, MASK, FIELD, MODE>(a, c, m, stages[0], mlpW, mlpX, mlpY, acc, qs);
+      __syncwarp();  // every lane done with its stage slots before they are refilled
+    } else {
+      cp_async_wait1();
       compute_pair<POT, MASK, FIELD, MODE>(a, c, m, stages[it & 1], acc, qs);
+    }
     units++;
   }
   asm volatile("cp.async.wait_all;" ::: "memory");

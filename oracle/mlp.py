@@ -188,12 +188,28 @@ def bf16_round(x):
     return r.astype(np.uint32).view(np.float32).astype(np.float64)
 
 
+def gelu_bf16_arith(h):
+    """GELU as the engine's inference kernel evaluates it: packed BF16
+    arithmetic, every operation rounded to bfloat16 (tanh itself exact here,
+    approximate in hardware), constants rounded to bfloat16."""
+    c = bf16_round(GELU_C)
+    c3 = bf16_round(GELU_C * 0.044715)
+    x = bf16_round(h)
+    x2 = bf16_round(x * x)
+    t = bf16_round(x2 * c3 + c)
+    u = bf16_round(x * t)
+    th = bf16_round(np.tanh(u))
+    hh = bf16_round(x * 0.5)
+    return bf16_round(hh * th + hh)
+
+
 def forward_bf16(params, X):
     """The forward pass with the engine's roundings: inputs, weights and hidden
-    activations as bfloat16, FP32-exact products accumulated in FP64."""
+    activations as bfloat16, FP32-exact products accumulated in FP64, GELU in
+    BF16 arithmetic (gelu_bf16_arith)."""
     W1, b1, W2, b2, W3, b3 = params
     H1 = bf16_round(X) @ bf16_round(W1) + b1
-    A1 = bf16_round(gelu(H1))
+    A1 = gelu_bf16_arith(H1)
     H2 = A1 @ bf16_round(W2) + b2
-    A2 = bf16_round(gelu(H2))
+    A2 = gelu_bf16_arith(H2)
     return A2 @ bf16_round(W3) + b3
