@@ -212,6 +212,27 @@ long long mcx_kernel_launches(const mcx_engine *eng);
 mcx_status mcx_set_staged(mcx_engine *eng, int on);
 int mcx_get_staged(const mcx_engine *eng);
 
+/* The kernel that runs the plain proposal's sweeps (all give bit-identical
+ * results):
+ *   MCX_PASS_MARCH   the default: a CTA marches a block of same-colour site
+ *                    pairs of one z-plane through a chunk of planes, keeping
+ *                    the z neighbours in registers;
+ *   MCX_PASS_DIRECT  persistent CTAs, each pair's neighbourhood loaded by
+ *                    cp.async into shared memory;
+ *   MCX_PASS_STAGED  the staged TMA pass above (mcx_set_staged).
+ * No counterpart in the reference. */
+typedef enum { MCX_PASS_MARCH = 0, MCX_PASS_DIRECT = 1, MCX_PASS_STAGED = 2 } mcx_pass_kind;
+mcx_status mcx_set_pass(mcx_engine *eng, int kind);
+int mcx_get_pass(const mcx_engine *eng);
+/* The z-march pass's shape: CTA size (64, 128 or 256 threads, one site pair
+ * each) and chunk depth (planes per CTA).  Default 128 x 8. */
+mcx_status mcx_set_march_shape(mcx_engine *eng, int block, int planes);
+/* Autotuner: times the z-march pass for block sizes {64, 128, 256} and chunk
+ * depths {1, 2, 4, ..., 32} (up to the deepest lattice) on a scratch copy of
+ * the engine's state (the state itself is untouched), keeps the fastest and
+ * reports it (any output may be NULL).  Synchronous. */
+mcx_status mcx_autotune(mcx_engine *eng, int *block, int *planes, float *pass_us);
+
 /* Learned proposal (no counterpart in the reference).  A small network reads
  * a site's six neighbour directors and T (19 inputs) and gives the mean axis
  * and log-concentration of an antipodal von Mises-Fisher mixture,

@@ -68,6 +68,12 @@ struct mcx_engine {
   uint8_t *d_mlp = nullptr;
   std::vector<float> mlp;  // FP32 weights as last set or trained
   int lgrid[4] = {0, 0, 0, 0};
+  // z-march pass (the default sweep pass of the plain proposal)
+  bool march = true;
+  int march_nt = 128, march_k = 8;
+  std::vector<int4> units;
+  int4 *d_units = nullptr;
+  long long dir_total = 0;  // floats of d_dir
   // training of the network: FP32 master weights, Adam moments, gradient
   float *d_w = nullptr, *d_am = nullptr, *d_av = nullptr, *d_g = nullptr, *d_loss = nullptr;
   bool w_stale = true;  // d_w does not hold e->mlp yet (Adam restarts)
@@ -78,6 +84,9 @@ struct mcx_engine {
   long long idx_cap = 0, repof_cap = 0, loss_bytes = 0;
   int held_samples = 0;  // samples in d_samples (last collection or mcx_mlp_grad upload)
 };
+
+static void drop_graphs(mcx_engine *e);
+static PassArgs pass_args(mcx_engine *e);
 
 static mcx_status fail(mcx_engine *e, mcx_status st, const char *fmt, ...) {
   char buf[512];
@@ -180,6 +189,7 @@ static void free_engine(mcx_engine *e) {
   cudaFree(e->d_tiles);
   cudaFree(e->d_err);
   cudaFree(e->d_mlp);
+  cudaFree(e->d_units);
   cudaFree(e->d_w);
   cudaFree(e->d_am);
   cudaFree(e->d_av);
@@ -214,6 +224,24 @@ static mcx_status check_desc(const mcx_replica_desc &d, int r) {
 static void effective_bounds(mcx_replica_desc &d) {
   if (d.geometry == MCX_GEO_SLAB) d.zbound = MCX_BOUND_FREE;
   if (d.geometry == MCX_GEO_SPHERE) d.xbound = d.ybound = d.zbound = MCX_BOUND_FREE;
+}
+
+// Work units of the z-march pass: per replica, blocks of march_nt pairs of a
+// plane times chunks of march_k planes, chunk-major so that the CTAs resident
+// together work on neighbouring planes.
+static void plan_march(mcx_engine *e) {
+  e->units.clear();
+  for (int r = 0; r < e->nrep; r++) {
+    RepDev &R = e->rep[r];
+    const int npp = R.hp * R.ny;
+    const int K = std::max(1, std::min(e->march_k, R.nz));
+    R.mcta = 0;
+    for (int k0 = 0; k0 < R.nz; k0 += K)
+      for (int p0 = 0; p0 < npp; p0 += e->march_nt) {
+        e->units.push_back(make_int4(r, p0, k0, std::min(K, R.nz - k0)));
+        R.mcta++;
+      }
+  }
 }
 
 extern "C" mcx_status mcx_create(int n, const mcx_replica_desc *descs, mcx_engine **out) {
@@ -298,6 +326,13 @@ extern "C" mcx_status mcx_create(int n, const mcx_replica_desc *descs, mcx_engin
   }
   for (int r = 0; r < n; r++) e->rep[r].ns_off = e->var.mask ? e->rep[r].dir_off : -1;
   {
+    const char *nt = getenv("MCX_MARCH_NT"), *kk = getenv("MCX_MARCH_K"), *mo = getenv("MCX_MARCH");
+    if (nt && march_block_ok(atoi(nt))) e->march_nt = atoi(nt);
+    if (kk && atoi(kk) > 0) e->march_k = atoi(kk);
+    if (mo && atoi(mo) == 0) e->march = false;
+    plan_march(e);
+  }
+  {
     const char *kb = getenv("MCX_STAGE_KB");
     const long long budget = (kb ? atoll(kb) : 40) * 1024;
     e->can_stage = true;
@@ -329,6 +364,7 @@ extern "C" mcx_status mcx_create(int n, const mcx_replica_desc *descs, mcx_engin
     }                                                                                              \
   } while (0)
   CKC(cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking));
+  e->dir_total = dir_total;
   CKC(cudaMalloc(&e->d_dir, sizeof(float) * dir_total));
   CKC(cudaMemsetAsync(e->d_dir, 0, sizeof(float) * dir_total, e->stream));
   if (e->var.mask) {
@@ -337,6 +373,8 @@ extern "C" mcx_status mcx_create(int n, const mcx_replica_desc *descs, mcx_engin
     CKC(cudaMalloc(&e->d_ns, sizeof(float) * dir_total));
     CKC(cudaMemsetAsync(e->d_ns, 0, sizeof(float) * dir_total, e->stream));
   }
+  CKC(cudaMalloc(&e->d_units, sizeof(int4) * e->units.size()));
+  CKC(cudaMemcpyAsync(e->d_units, e->units.data(), sizeof(int4) * e->units.size(), cudaMemcpyHostToDevice, e->stream));
   CKC(cudaMalloc(&e->d_rep, sizeof(RepDev) * n));
   CKC(cudaMalloc(&e->d_map, sizeof(int2) * e->map.size()));
   CKC(cudaMalloc(&e->d_st, sizeof(RepState) * n));
@@ -584,6 +622,8 @@ static PassArgs pass_args(mcx_engine *e) {
   pa.ntiles = (int)e->tiles.size();
   pa.stage_bytes = e->stage_bytes;
   pa.err = e->d_err;
+  pa.units = e->d_units;
+  pa.nunits = (int)e->units.size();
   return pa;
 }
 
@@ -593,6 +633,7 @@ static void launch_sweep_pass(mcx_engine *e, PassArgs &pa, int colour, bool meas
   const int mode = measure ? MODE_SWEEP_MEASURE : MODE_SWEEP;
   if (e->proposal == MCX_PROPOSAL_VMF_MLP) launch_pass_learned(e->var, mode, pa, e->lgrid[mode], e->stream);
   else if (e->staged) launch_tpass(e->var, mode, pa, e->grid[measure ? 1 : 0], e->stream);
+  else if (e->march) launch_march(e->var, mode, pa, e->march_nt, e->stream);
   else launch_pass(e->var, mode, pa, e->pgrid[mode], e->stream);
 }
 
@@ -678,11 +719,14 @@ extern "C" mcx_status mcx_sync(mcx_engine *e) {
   return check_err_flag(e);
 }
 
-extern "C" mcx_status mcx_set_staged(mcx_engine *e, int on) {
+extern "C" mcx_status mcx_set_pass(mcx_engine *e, int kind) {
   if (!e) return fail(nullptr, MCX_ERR_INVALID, "null engine");
-  if (on && !e->can_stage) return fail(e, MCX_ERR_UNSUPPORTED, "a replica's rows do not fit the staged pass's shared memory");
+  if (kind < MCX_PASS_MARCH || kind > MCX_PASS_STAGED) return fail(e, MCX_ERR_INVALID, "unknown pass kernel %d", kind);
+  if (kind == MCX_PASS_STAGED && !e->can_stage)
+    return fail(e, MCX_ERR_UNSUPPORTED, "a replica's rows do not fit the staged pass's shared memory");
   CK(e, cudaStreamSynchronize(e->stream));
-  e->staged = on != 0;
+  e->staged = kind == MCX_PASS_STAGED;
+  e->march = kind == MCX_PASS_MARCH;
   for (int m = 0; m < 2; m++)
     if (e->graph[m]) {
       cudaGraphExecDestroy(e->graph[m]);
@@ -691,7 +735,129 @@ extern "C" mcx_status mcx_set_staged(mcx_engine *e, int on) {
   return MCX_OK;
 }
 
+extern "C" int mcx_get_pass(const mcx_engine *e) {
+  if (!e) return -1;
+  return e->staged ? MCX_PASS_STAGED : (e->march ? MCX_PASS_MARCH : MCX_PASS_DIRECT);
+}
+
+extern "C" mcx_status mcx_set_staged(mcx_engine *e, int on) {
+  return mcx_set_pass(e, on ? MCX_PASS_STAGED : MCX_PASS_MARCH);
+}
+
 extern "C" int mcx_get_staged(const mcx_engine *e) { return e && e->staged ? 1 : 0; }
+
+// Re-plans the z-march units for a block size and chunk depth and uploads
+// them with the replicas' CTA counts.
+static mcx_status apply_march_shape(mcx_engine *e, int nt, int k) {
+  e->march_nt = nt;
+  e->march_k = k;
+  const size_t before = e->units.size();
+  plan_march(e);
+  if (e->units.size() > before || !e->d_units) {
+    cudaFree(e->d_units);
+    e->d_units = nullptr;
+    CK(e, cudaMalloc(&e->d_units, sizeof(int4) * e->units.size()));
+  }
+  CK(e, cudaMemcpyAsync(e->d_units, e->units.data(), sizeof(int4) * e->units.size(), cudaMemcpyHostToDevice, e->stream));
+  CK(e, cudaMemcpyAsync(e->d_rep, e->rep.data(), sizeof(RepDev) * e->nrep, cudaMemcpyHostToDevice, e->stream));
+  CK(e, cudaStreamSynchronize(e->stream));
+  drop_graphs(e);
+  return MCX_OK;
+}
+
+extern "C" mcx_status mcx_set_march_shape(mcx_engine *e, int block, int planes) {
+  if (!e) return fail(nullptr, MCX_ERR_INVALID, "null engine");
+  if (!march_block_ok(block) || planes < 1) return fail(e, MCX_ERR_INVALID, "z-march shape %d threads x %d planes", block, planes);
+  CK(e, cudaStreamSynchronize(e->stream));
+  return apply_march_shape(e, block, planes);
+}
+
+// Times the z-march pass for every candidate shape on a scratch copy of the
+// directors and per-replica state (the engine's own state is untouched) and
+// keeps the fastest.
+extern "C" mcx_status mcx_autotune(mcx_engine *e, int *block, int *planes, float *pass_us) {
+  if (!e) return fail(nullptr, MCX_ERR_INVALID, "null engine");
+  CK(e, cudaStreamSynchronize(e->stream));
+  int maxnz = 1;
+  for (const RepDev &R : e->rep) maxnz = std::max(maxnz, R.nz);
+  float *d_dir = nullptr;
+  RepState *d_st = nullptr;
+  double *d_stats = nullptr, *d_ring = nullptr;
+  const size_t ring_n = (size_t)e->nrep * (e->ring_cap + 1) * kLanes * kQ;
+  cudaEvent_t t0, t1;
+  mcx_status st = MCX_OK;
+  int best_nt = e->march_nt, best_k = e->march_k;
+  float best = 1e30f;
+#define CKA(call)                                                                                    \
+  do {                                                                                               \
+    cudaError_t _r = (call);                                                                         \
+    if (_r != cudaSuccess) {                                                                         \
+      st = fail(e, MCX_ERR_CUDA, "autotune: %s: %s", #call, cudaGetErrorString(_r));                 \
+      goto done;                                                                                     \
+    }                                                                                                \
+  } while (0)
+  CKA(cudaEventCreate(&t0));
+  CKA(cudaEventCreate(&t1));
+  CKA(cudaMalloc(&d_dir, sizeof(float) * e->dir_total));
+  CKA(cudaMalloc(&d_st, sizeof(RepState) * e->nrep));
+  CKA(cudaMalloc(&d_stats, sizeof(double) * kStats * e->nrep));
+  CKA(cudaMalloc(&d_ring, sizeof(double) * ring_n));
+  CKA(cudaMemcpyAsync(d_dir, e->d_dir, sizeof(float) * e->dir_total, cudaMemcpyDeviceToDevice, e->stream));
+  CKA(cudaMemcpyAsync(d_st, e->d_st, sizeof(RepState) * e->nrep, cudaMemcpyDeviceToDevice, e->stream));
+  {
+    const int nts[3] = {64, 128, 256};
+    for (int a = 0; a < 3; a++)
+      for (int k = 1; k <= 32; k *= 2) {
+        if (k > maxnz && k > 1) break;
+        if ((st = apply_march_shape(e, nts[a], k))) goto done;
+        PassArgs pa = pass_args(e);
+        pa.dir = d_dir;
+        pa.st = d_st;
+        pa.stats = d_stats;
+        pa.ring = d_ring;
+        const int reps = 8;
+        for (int w = 0; w < 2; w++)
+          for (int c = 0; c < 2; c++) {
+            pa.colour = c;
+            launch_march(e->var, MODE_SWEEP, pa, nts[a], e->stream);
+          }
+        CKA(cudaEventRecord(t0, e->stream));
+        for (int q = 0; q < reps; q++)
+          for (int c = 0; c < 2; c++) {
+            pa.colour = c;
+            launch_march(e->var, MODE_SWEEP, pa, nts[a], e->stream);
+          }
+        CKA(cudaEventRecord(t1, e->stream));
+        CKA(cudaGetLastError());
+        CKA(cudaEventSynchronize(t1));
+        e->launches += 4 + 2 * reps;
+        float ms = 0.f;
+        CKA(cudaEventElapsedTime(&ms, t0, t1));
+        const float us = ms * 1e3f / (2 * reps);
+        if (us < best) {
+          best = us;
+          best_nt = nts[a];
+          best_k = k;
+        }
+      }
+  }
+  st = apply_march_shape(e, best_nt, best_k);
+done:
+#undef CKA
+  cudaStreamSynchronize(e->stream);
+  cudaFree(d_dir);
+  cudaFree(d_st);
+  cudaFree(d_stats);
+  cudaFree(d_ring);
+  cudaEventDestroy(t0);
+  cudaEventDestroy(t1);
+  if (st == MCX_OK) {
+    if (block) *block = best_nt;
+    if (planes) *planes = best_k;
+    if (pass_us) *pass_us = best;
+  }
+  return st;
+}
 
 static void drop_graphs(mcx_engine *e) {
   for (int m = 0; m < 2; m++)

@@ -50,6 +50,9 @@ struct PassArgs {
   int ntiles;
   int stage_bytes;
   unsigned *err;  // set to 1 when a shared-memory copy did not arrive in time
+  // z-march pass: (replica, first pair of the plane, first plane, planes)
+  const int4 *units;
+  int nunits;
 };
 
 struct FlushArgs {
@@ -66,6 +69,9 @@ struct FlushArgs {
 // The direct pass over a.map with `nblocks` persistent CTAs.
 void launch_pass(const Variant &v, int mode, const PassArgs &a, int nblocks, cudaStream_t st);
 int pass_blocks_per_sm(const Variant &v, int mode);
+// The z-march pass (mcx_march.cu): one CTA of nt threads per unit of a.units.
+void launch_march(const Variant &v, int mode, const PassArgs &a, int nt, cudaStream_t st);
+bool march_block_ok(int nt);
 // The direct pass with the learned proposal (mcx_learned.cu).
 void launch_pass_learned(const Variant &v, int mode, const PassArgs &a, int nblocks, cudaStream_t st);
 int pass_learned_blocks_per_sm(const Variant &v, int mode);

@@ -20,7 +20,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 PKG = os.path.dirname(HERE)
-LIB_PATH = os.path.join(PKG, "_build", "libmcx.so")
+LIB_PATH = os.environ.get("MCX_LIB") or os.path.join(PKG, "_build", "libmcx.so")
 CLI_PATH = os.path.join(PKG, "_build", "mc_sim_gb300")
 
 MAX_SURFACES = 16
@@ -30,6 +30,7 @@ BOUNDS = {"free": 0, "periodic": 1}
 ANCHORINGS = {"homeotropic": 0, "fg": 1, "rp": 2, "strong": 3, "homeotropic_ghrl": 4, "fg_ghrl": 5, "rp_ghrl": 6,
               "strong_ghrl": 7}
 PROPOSALS = {"plain": 0, "vmf_mlp": 1}
+PASSES = {"march": 0, "direct": 1, "staged": 2}
 MLP_PARAMS = 6792
 SAMPLE_FLOATS = 24
 AUG_FLIP, AUG_ROTATE = 1, 2
@@ -139,6 +140,10 @@ def lib() -> C.CDLL:
         L.mcx_kernel_launches.restype = C.c_longlong
         L.mcx_run_file.argtypes = [C.c_char_p, C.c_char_p]
         L.mcx_set_staged.argtypes = [V, I]
+        L.mcx_set_pass.argtypes = [V, I]
+        L.mcx_get_pass.argtypes = [V]
+        L.mcx_set_march_shape.argtypes = [V, I, I]
+        L.mcx_autotune.argtypes = [V, C.POINTER(I), C.POINTER(I), C.POINTER(F)]
         L.mcx_get_staged.argtypes = [V]
         L.mcx_stream.argtypes = [V]
         L.mcx_stream.restype = V
@@ -333,6 +338,24 @@ class Engine:
         loss = np.zeros(1, np.float32)
         self._ck(self._L.mcx_mlp_grad(self._h, _p(s), int(s.shape[0]), _p(g), _p(loss)))
         return float(loss[0]), g
+
+    @property
+    def pass_kind(self) -> str:
+        return {0: "march", 1: "direct", 2: "staged"}[int(self._L.mcx_get_pass(self._h))]
+
+    @pass_kind.setter
+    def pass_kind(self, kind: str):
+        self._ck(self._L.mcx_set_pass(self._h, PASSES[kind]))
+
+    def set_march_shape(self, block: int, planes: int):
+        self._ck(self._L.mcx_set_march_shape(self._h, int(block), int(planes)))
+
+    def autotune(self):
+        """Chooses the z-march pass's block size and chunk depth by timing;
+        returns (block, planes, microseconds per pass)."""
+        b, k, us = C.c_int(), C.c_int(), C.c_float()
+        self._ck(self._L.mcx_autotune(self._h, C.byref(b), C.byref(k), C.byref(us)))
+        return b.value, k.value, us.value
 
     @property
     def staged(self) -> bool:

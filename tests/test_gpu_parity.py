@@ -238,28 +238,88 @@ def test_errors_are_status_codes():
             e.set_field(1.0)
 
 
+KERNELS = [("march", 128, 8), ("march", 64, 1), ("march", 256, 32), ("march", 128, 3), ("direct", 0, 0),
+           ("staged", 0, 0)]
+
+
+def _run_kernel(descs, setup, kind, block, planes, sweeps=19):
+    with mcx.Engine(descs) as eng:
+        if kind == "staged":
+            try:
+                eng.pass_kind = "staged"
+            except mcx.McxError:
+                return None
+        else:
+            eng.pass_kind = kind
+        assert eng.pass_kind == kind
+        if kind == "march":
+            eng.set_march_shape(block, planes)
+        setup(eng)
+        eng.sweep(sweeps, measure=True)
+        return [(eng.get_state(r), eng.stats(r)) for r in range(len(descs))]
+
+
+def _assert_same(out_a, out_b):
+    for (sa, ta), (sb, tb) in zip(out_a, out_b):
+        assert np.array_equal(sa, sb)
+        assert ta[mcx.ST_ANG_VAR] == tb[mcx.ST_ANG_VAR]
+        assert ta[mcx.ST_ACC] == tb[mcx.ST_ACC]
+        assert ta[mcx.ST_S1] == pytest.approx(tb[mcx.ST_S1], rel=1e-6)
+        assert ta[mcx.ST_E1] == pytest.approx(tb[mcx.ST_E1], rel=1e-6)
+
+
 @pytest.mark.parametrize("name", list(CASES))
-def test_staged_and_direct_kernels_agree(name):
-    """The staged (TMA, shared-memory) pass and the direct pass compute the
-    same thing: bit-identical states and step sizes after measured sweeps."""
+def test_pass_kernels_agree(name):
+    """The z-march pass (several shapes), the direct pass and the staged (TMA)
+    pass compute the same thing: bit-identical states, step sizes and
+    acceptance counts after measured sweeps."""
     m = CASES[name]
-    rng = np.random.default_rng(5 + sum(name.encode()))
     d = desc_from_model(m, T=0.95, seed=21, stream=2)
-    out = []
-    for staged in (True, False):
-        with mcx.Engine([d]) as eng:
-            eng.staged = staged
-            assert eng.staged == staged
-            if m.geometry == "custom":
-                pt, ns = _custom_mask(m, np.random.default_rng(3))
-                eng.set_mask(0, pt, ns)
-            else:
-                pt = O.Lattice(m).pt
-            eng.set_state(0, random_state(m, pt, np.random.default_rng(7)))
-            eng.sweep(19, measure=True)
-            out.append((eng.get_state(0), eng.stats(0)))
-    (sa, ta), (sb, tb) = out
-    assert np.array_equal(sa, sb)
-    assert ta[mcx.ST_ANG_VAR] == tb[mcx.ST_ANG_VAR]
-    assert ta[mcx.ST_S1] == pytest.approx(tb[mcx.ST_S1], rel=1e-6)
-    assert ta[mcx.ST_E1] == pytest.approx(tb[mcx.ST_E1], rel=1e-6)
+
+    def setup(eng):
+        if m.geometry == "custom":
+            pt, ns = _custom_mask(m, np.random.default_rng(3))
+            eng.set_mask(0, pt, ns)
+        else:
+            pt = O.Lattice(m).pt
+        eng.set_state(0, random_state(m, pt, np.random.default_rng(7)))
+
+    ref = _run_kernel([d], setup, "direct", 0, 0)
+    for kind, block, planes in KERNELS:
+        out = _run_kernel([d], setup, kind, block, planes)
+        if out is not None:
+            _assert_same(ref, out)
+
+
+def test_pass_kernels_agree_on_uneven_batch():
+    """A batch of replicas of different sizes and bounds in one launch: the
+    z-march units of each replica end where the next begins."""
+    models = [O.Model(nx=16, ny=16, nz=16, potential="ll"), O.Model(nx=24, ny=8, nz=12, potential="ll", A=1.2),
+              O.Model(nx=10, ny=6, nz=4, xbound="free", ybound="free", zbound="free", potential="ll"),
+              O.Model(nx=32, ny=30, nz=6, potential="ll")]
+    descs = [desc_from_model(m, T=0.9 + 0.05 * r, seed=40 + r, stream=r) for r, m in enumerate(models)]
+
+    def setup(eng):
+        for r, m in enumerate(models):
+            eng.set_state(r, random_state(m, np.ones(m.n, np.int32), np.random.default_rng(r)))
+
+    ref = _run_kernel(descs, setup, "direct", 0, 0, sweeps=21)
+    for kind, block, planes in KERNELS[:4]:
+        _assert_same(ref, _run_kernel(descs, setup, kind, block, planes, sweeps=21))
+
+
+def test_autotune_keeps_state_and_results():
+    m = O.Model(nx=32, ny=32, nz=32, potential="ll")
+    d = desc_from_model(m, T=1.0, seed=8, stream=1)
+    ni0 = random_state(m, np.ones(m.n, np.int32), np.random.default_rng(2))
+    with mcx.Engine([d]) as a, mcx.Engine([d]) as b:
+        a.set_state(0, ni0)
+        b.set_state(0, ni0)
+        block, planes, us = a.autotune()
+        assert block in (64, 128, 256) and 1 <= planes <= 32 and us > 0
+        assert np.array_equal(a.get_state(0), ni0)
+        assert a.stats(0)[mcx.ST_SWEEP_INDEX] == 0
+        a.sweep(40, measure=True)
+        b.sweep(40, measure=True)
+        assert np.array_equal(a.get_state(0), b.get_state(0))
+        assert a.stats(0)[mcx.ST_ANG_VAR] == b.stats(0)[mcx.ST_ANG_VAR]
