@@ -252,14 +252,22 @@ def main():
                     help="lattice side (default 128, the headline workload; other sides are for profiling)")
     ap.add_argument("--sweeps", type=int, default=2000,
                     help="MCT = MCS per temperature (default 2000, the headline workload)")
+    ap.add_argument("--replicas", type=int, default=1,
+                    help="independent lattices in one engine (default 1, the headline workload; more for profiling "
+                         "the batched pass)")
+    ap.add_argument("--proposal", default="plain", choices=["plain", "vmf_mlp"],
+                    help="plain (the reference's move; default) or the learned proposal with untrained weights "
+                         "(for profiling its pass)")
     args = ap.parse_args()
     global NX, NY, NZ, SITES, MCT, MCS, WORKLOAD
-    if args.side != 128 or args.sweeps != 2000:
+    R = max(1, args.replicas)
+    if args.side != 128 or args.sweeps != 2000 or R != 1 or args.proposal != "plain":
         NX = NY = NZ = args.side
         SITES = NX * NY * NZ
         MCT = MCS = args.sweeps
-        WORKLOAD = (f"LL bulk {NX}^3 periodic, A=1, homogeneous ic along z, anneal Ti=1.20 -> Tf=0.90 dT=-0.01, "
-                    f"MCT={MCT} MCS={MCS} per temperature (profiling variant of the headline workload)")
+        WORKLOAD = (f"LL bulk {NX}^3 periodic x {R} replicas, A=1, homogeneous ic along z, anneal Ti=1.20 -> "
+                    f"Tf=0.90 dT=-0.01, MCT={MCT} MCS={MCS} per temperature, {args.proposal} proposal (profiling "
+                    f"variant of the headline workload)")
     ws, rank, lrank = dist_info()
     if args.impl == "reference":
         run_reference(args, ws, rank)
@@ -273,18 +281,24 @@ def main():
     import mcx
 
     temps = temperatures()
-    desc = mcx.replica(nx=NX, ny=NY, nz=NZ, potential="ll", A=1.0, T=temps[0], ang_var=0.5, seed=1 + rank,
-                       stream=rank)
-    eng = mcx.Engine([desc])
+    descs = [mcx.replica(nx=NX, ny=NY, nz=NZ, potential="ll", A=1.0, T=temps[0], ang_var=0.5, seed=1 + rank * R + q,
+                         stream=rank * R + q) for q in range(R)]
+    eng = mcx.Engine(descs)
     stream = torch.cuda.ExternalStream(mcx.lib().mcx_stream(eng._h))
     # the engine's autotuner picks the z-march pass shape (on a scratch copy of
     # the state, before anything is timed)
-    eng.init_homogeneous(0, 0.0, 0.0)
+    for q in range(R):
+        eng.init_homogeneous(q, 0.0, 0.0)
     tuned = eng.autotune()
+    if args.proposal != "plain":
+        from mcx import gain
+        eng.set_mlp(gain.init_weights(1))
+        eng.set_proposal(args.proposal)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
 
     def reset():
-        eng.init_homogeneous(0, 0.0, 0.0)
+        for q in range(R):
+            eng.init_homogeneous(q, 0.0, 0.0)
         eng.set_step(0.5)
 
     def block(T):
@@ -332,7 +346,7 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         total_ms = float(t.item())
     per_step_ms = total_ms / nsteps
-    updates_per_step = (MCT + MCS) * SITES
+    updates_per_step = (MCT + MCS) * SITES * R
     value = ws * updates_per_step * nsteps / (total_ms / 1e3)
 
     # live pass-kernel timing for the roofline
@@ -343,7 +357,7 @@ def main():
     if st:
         raise RuntimeError(mcx.lib().mcx_last_error(eng._h).decode())
     per_launch_ms = pass_ms.value / (2 * n_prof)
-    bytes_per_launch = BYTES_PER_SITE_PASS * SITES
+    bytes_per_launch = BYTES_PER_SITE_PASS * SITES * R
     achieved = bytes_per_launch / (per_launch_ms * 1e-3) / 1e9
     peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(peaks_path):
@@ -352,7 +366,7 @@ def main():
     else:
         peak, peak_src = 6800.0, "fallback"
     traffic = None
-    tpath = os.path.join(ROOT, "profiles", f"sweep_pass_ll{NX}.md")
+    tpath = os.path.join(ROOT, "profiles", f"sweep_pass_ll{NX}.md" if R == 1 else f"sweep_pass_ll{NX}x{R}.md")
     if os.path.exists(tpath):
         for ln in open(tpath):
             if ln.startswith("dram_bytes_per_launch:"):
@@ -375,20 +389,22 @@ def main():
         eng.set_step(0.5)
         t0 = time.perf_counter()
         for s in range(nsteps):
-            if L.mcx_set_state(eng._h, 0, pin):
-                raise RuntimeError(L.mcx_last_error(eng._h).decode())
+            for q in range(R):
+                if L.mcx_set_state(eng._h, q, pin):
+                    raise RuntimeError(L.mcx_last_error(eng._h).decode())
             block(temps[s % len(temps)])
             if L.mcx_get_stats(eng._h, 0, stats.ctypes.data_as(C2.c_void_p)):
                 raise RuntimeError(L.mcx_last_error(eng._h).decode())
-            if L.mcx_get_state(eng._h, 0, pout):
-                raise RuntimeError(L.mcx_last_error(eng._h).decode())
+            for q in range(R):
+                if L.mcx_get_state(eng._h, q, pout):
+                    raise RuntimeError(L.mcx_last_error(eng._h).decode())
         e2e_s = time.perf_counter() - t0
         if dist:
             t = torch.tensor([e2e_s], device="cuda")
             dist.all_reduce(t, op=dist.ReduceOp.MAX)
             e2e_s = float(t.item())
         e2e = {"value": ws * updates_per_step * nsteps / e2e_s, "unit": "site-updates/s",
-               "h2d_bytes_per_step": 12 * SITES, "d2h_bytes_per_step": 12 * SITES + 16 * 8}
+               "h2d_bytes_per_step": 12 * SITES * R, "d2h_bytes_per_step": 12 * SITES * R + 16 * 8}
 
     if rank != 0:
         eng.close()
@@ -404,7 +420,7 @@ def main():
                    "step": f"one temperature block: {MCT} sweeps + {MCS} sweeps each followed by FP64 E/Q/S",
                    "l2": "flushed (256 MiB write) between steps outside the timed windows; the 25 MB lattice "
                          "stays L2-resident within a step",
-                   "parallelism": f"replicas x{ws}" if ws > 1 else "single lattice",
+                   "parallelism": (f"replicas x{ws} ranks" if ws > 1 else "one GPU") + f", {R} lattice(s) per engine",
                    "pass_kernel": f"z-march, {tuned[0]} threads x {tuned[1]} planes per CTA (autotuned)",
                    "S_E_last_step": [rows[-1][0], rows[-1][1], rows[-1][2]] if rows else None},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
