@@ -136,3 +136,25 @@ def run(L: int = 96, temps: Sequence[float] = (1.00, 1.10, 1.12, 1.15), per_T: i
         out["mlp_tflops"] = runs["vmf_mlp"]["sweeps_per_s"] * sites * MLP_FLOP_PER_UPDATE / 1e12
         out["parity_3sigma"] = all(r["E_diff_sigma"] < 3 and r["S_diff_sigma"] < 3 for r in rows)
     return out
+
+
+if __name__ == "__main__":
+    import argparse
+    import json
+
+    ap = argparse.ArgumentParser(description="learned vs plain proposal: independent samples/s")
+    ap.add_argument("--side", type=int, default=96)
+    ap.add_argument("--per-T", type=int, default=32)
+    ap.add_argument("--equil", type=int, default=6000)
+    ap.add_argument("--meas", type=int, default=12000)
+    ap.add_argument("--samples", type=int, default=1_000_000)
+    ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--out", default=None)
+    a = ap.parse_args()
+    res = run(L=a.side, per_T=a.per_T, equil=a.equil, meas=a.meas, train_samples=a.samples, seed=a.seed,
+              log=lambda m: print(m, flush=True))
+    txt = json.dumps(res)
+    if a.out:
+        with open(a.out, "w") as f:
+            f.write(txt + "\n")
+    print(txt)
