@@ -421,10 +421,11 @@ def main():
                    "l2": "flushed (256 MiB write) between steps outside the timed windows; the 25 MB lattice "
                          "stays L2-resident within a step",
                    "parallelism": (f"replicas x{ws} ranks" if ws > 1 else "one GPU") + f", {R} lattice(s) per engine",
-                   "pass_kernel": f"z-march, {tuned[0]} threads x {tuned[1]} planes per CTA (autotuned)",
+                   "pass_kernel": (f"z-march, {tuned[0]} threads x {tuned[1]} planes per CTA (autotuned)"
+                                   if args.proposal == "plain" else "learned-proposal pass (k_pass, BF16 MLP)"),
                    "S_E_last_step": [rows[-1][0], rows[-1][1], rows[-1][2]] if rows else None},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": traffic, "peak_source": peak_src, "kernel": "k_march<LL> (red/black pass)",
+                     "traffic": traffic, "peak_source": peak_src, "kernel": "k_march<LL> (red/black pass)" if args.proposal == "plain" else "k_pass<LL, learned>",
                      "bytes_per_launch": bytes_per_launch, "launch_ms": per_launch_ms,
                      "pass_share_of_sweep": pass_ms.value / all_ms.value if all_ms.value else None},
         "cpu_baseline": cpu,

@@ -362,3 +362,29 @@ def sweep_uniforms(model: Model, pt: np.ndarray, seed: int, stream: int, sweep: 
         for site in s[m]:
             out.append(site_uniforms(nx, ny, int(site), seed, stream, sweep, tag=tag))
     return np.array(out, dtype=np.float64).reshape(-1)
+
+
+def anneal(model: Model, temps: Sequence[float], mct: int, mcs: int, seed: int, stream: int, ni0: np.ndarray,
+           order: str = "redblack") -> np.ndarray:
+    """thermalEvolveN::run (src/evolve_thermal.cpp:30-99) on the oracle: per
+    temperature mct sweeps, then mcs sweeps each followed by E and S; the
+    step size (starting at 0.5) carries across temperatures.  Returns rows
+    (T, mean S, mean E)."""
+    lat = Lattice(model)
+    lat.ni[:] = ni0
+    a = np.float32(0.5)
+    sw = 0
+    rows = []
+    for T in temps:
+        for _ in range(mct):
+            _, a = lat.sweep(T, a, seed, stream, sw, order)
+            sw += 1
+        S1 = E1 = 0.0
+        for _ in range(mcs):
+            _, a = lat.sweep(T, a, seed, stream, sw, order)
+            sw += 1
+            r = lat.measure()
+            S1 += r["S"]
+            E1 += r["E"]
+        rows.append((T, S1 / mcs, E1 / mcs))
+    return np.array(rows)

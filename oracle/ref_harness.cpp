@@ -222,3 +222,9 @@ extern "C" float ref_order(const float *ni, float Q[9], float vec[3]) {
 }
 
 extern "C" int ref_max_threads(void) { return (int)RNG.size(); }
+
+/* Re-seeds the per-thread generators as thermalEvolveN::run does
+ * (src/evolve_thermal.cpp:40-45): seed * 104729 + thread. */
+extern "C" void ref_seed(unsigned long seed) {
+  for (size_t t = 0; t < RNG.size(); t++) gsl_rng_set(RNG[t], seed * 104729 + t);
+}

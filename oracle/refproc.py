@@ -102,6 +102,28 @@ def _worker(m: dict, ops: List[tuple]) -> List[Any]:
         elif kind == "energy":
             ni = np.ascontiguousarray(op[1], np.float32)
             out.append(float(L.ref_energy(_p(ni))))
+        elif kind == "anneal":
+            # thermalEvolveN::run (src/evolve_thermal.cpp:30-99): per temperature
+            # MCT sweeps, then MCS sweeps each followed by energy_calculator and
+            # the order parameter; the step size carries across temperatures.
+            ni = np.ascontiguousarray(op[1], np.float32).copy()
+            temps, mct, mcs, seed, nth = op[2], op[3], op[4], op[5], op[6]
+            L.ref_seed.argtypes = [C.c_ulong]
+            L.ref_seed(seed)
+            a = C.c_float(0.5)
+            rows = []
+            Q = np.zeros(9, np.float32)
+            v = np.zeros(3, np.float32)
+            for T in temps:
+                for _ in range(mct):
+                    L.ref_sweep(_p(ni), C.c_float(T), C.byref(a), None, 0, nth)
+                S1 = E1 = 0.0
+                for _ in range(mcs):
+                    L.ref_sweep(_p(ni), C.c_float(T), C.byref(a), None, 0, nth)
+                    E1 += float(L.ref_energy(_p(ni)))
+                    S1 += float(L.ref_order(_p(ni), _p(Q), _p(v)))
+                rows.append((T, S1 / mcs, E1 / mcs))
+            out.append(np.array(rows))
         elif kind == "order":
             ni = np.ascontiguousarray(op[1], np.float32)
             Q = np.zeros(9, np.float32)
