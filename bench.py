@@ -351,12 +351,22 @@ def main():
 
     # live pass-kernel timing for the roofline
     import ctypes as C
-    pass_ms, all_ms = C.c_float(), C.c_float()
-    n_prof = 200
-    st = mcx.lib().mcx_pass_timing(eng._h, n_prof, C.byref(pass_ms), C.byref(all_ms))
+    # (a) the pass kernel's average duration in the production sequence: 400
+    # unmeasured sweeps replayed from the engine's graphs between two events
+    # on its stream (launch gaps included, so this is conservative); (b) for
+    # reference, the mean of per-launch event brackets around directly
+    # launched passes (these include the host submission gap of each launch)
+    sw_ms = C.c_float()
+    n_prof = 400
+    st = mcx.lib().mcx_sweep_timing(eng._h, n_prof, C.byref(sw_ms))
     if st:
         raise RuntimeError(mcx.lib().mcx_last_error(eng._h).decode())
-    per_launch_ms = pass_ms.value / (2 * n_prof)
+    per_launch_ms = sw_ms.value / (2 * n_prof)
+    pass_ms, all_ms = C.c_float(), C.c_float()
+    st = mcx.lib().mcx_pass_timing(eng._h, 100, C.byref(pass_ms), C.byref(all_ms))
+    if st:
+        raise RuntimeError(mcx.lib().mcx_last_error(eng._h).decode())
+    per_launch_isolated_ms = pass_ms.value / 200
     bytes_per_launch = BYTES_PER_SITE_PASS * SITES * R
     achieved = bytes_per_launch / (per_launch_ms * 1e-3) / 1e9
     peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
@@ -427,6 +437,9 @@ def main():
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "peak_source": peak_src, "kernel": "k_march<LL> (red/black pass)" if args.proposal == "plain" else "k_pass<LL, learned>",
                      "bytes_per_launch": bytes_per_launch, "launch_ms": per_launch_ms,
+                     "launch_ms_isolated": per_launch_isolated_ms,
+                     "launch_ms_method": "400 graph-replayed unmeasured sweeps between two CUDA events on the "
+                                         "engine stream / 800 pass launches (launch gaps included)",
                      "pass_share_of_sweep": pass_ms.value / all_ms.value if all_ms.value else None},
         "cpu_baseline": cpu,
         "e2e": e2e,

@@ -308,6 +308,12 @@ void *mcx_stream(mcx_engine *eng);
  * the 2*n_sweeps pass kernels, total_ms the whole sequence.  For profiling:
  * the sweeps are real (state, RNG counter and step size advance). */
 mcx_status mcx_pass_timing(mcx_engine *eng, int n_sweeps, float *pass_ms, float *total_ms);
+/* n_sweeps unmeasured sweeps through mcx_sweep's own path (captured graphs of
+ * 16 sweeps) between two CUDA events on the engine's stream; ms receives the
+ * elapsed time.  Divided by 2*n_sweeps it is the pass kernel's average
+ * duration in the production launch sequence, launch gaps included.  The
+ * sweeps are real (state, RNG counter and step size advance). */
+mcx_status mcx_sweep_timing(mcx_engine *eng, int n_sweeps, float *ms);
 
 /* Host-only helpers (no GPU needed). */
 /* setGHRL (src/io.cpp:277-302): out = lambda, mu, nu, rho, sigma. */

@@ -263,6 +263,7 @@ extern "C" mcx_status mcx_create(int n, const mcx_replica_desc *descs, mcx_engin
   e->var.pot = descs[0].potential;
   e->var.mask = false;
   e->var.field = false;
+  e->var.per = true;
   long long dir_total = 0, pt_total = 0;
   e->rep.resize(n);
   for (int r = 0; r < n; r++) {
@@ -316,6 +317,9 @@ extern "C" mcx_status mcx_create(int n, const mcx_replica_desc *descs, mcx_engin
       R.dz[s] = ax[2];
     }
     if (d.geometry != MCX_GEO_BULK) e->var.mask = true;
+    if (d.xbound != MCX_BOUND_PERIODIC || d.ybound != MCX_BOUND_PERIODIC || d.zbound != MCX_BOUND_PERIODIC ||
+        d.nx % 4 != 0)
+      e->var.per = false;
     if (d.elecA != 0.f) e->var.field = true;
     e->max_sites = std::max(e->max_sites, (long long)R.ntot);
     R.ncta = 0;
@@ -324,6 +328,7 @@ extern "C" mcx_status mcx_create(int n, const mcx_replica_desc *descs, mcx_engin
       R.ncta++;
     }
   }
+  if (e->var.mask) e->var.per = false;
   for (int r = 0; r < n; r++) e->rep[r].ns_off = e->var.mask ? e->rep[r].dir_off : -1;
   {
     const char *nt = getenv("MCX_MARCH_NT"), *kk = getenv("MCX_MARCH_K"), *mo = getenv("MCX_MARCH");
@@ -1139,6 +1144,26 @@ extern "C" mcx_status mcx_get_series(mcx_engine *e, int r, int count, double *ou
 }
 
 extern "C" void *mcx_stream(mcx_engine *e) { return e ? (void *)e->stream : nullptr; }
+
+extern "C" mcx_status mcx_sweep_timing(mcx_engine *e, int n, float *ms) {
+  if (!e) return fail(nullptr, MCX_ERR_INVALID, "null engine");
+  if (n <= 0 || !ms) return fail(e, MCX_ERR_INVALID, "need n_sweeps > 0 and an output");
+  cudaEvent_t a, b;
+  CK(e, cudaEventCreate(&a));
+  CK(e, cudaEventCreate(&b));
+  mcx_status st = MCX_OK;
+  {
+    cudaError_t r = cudaEventRecord(a, e->stream);
+    if (r == cudaSuccess) st = run_sweeps(e, n, 0);
+    if (r == cudaSuccess && !st) r = cudaEventRecord(b, e->stream);
+    if (r == cudaSuccess && !st) r = cudaEventSynchronize(b);
+    if (r == cudaSuccess && !st) r = cudaEventElapsedTime(ms, a, b);
+    if (r != cudaSuccess && !st) st = fail(e, MCX_ERR_CUDA, "mcx_sweep_timing: %s", cudaGetErrorString(r));
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  return st;
+}
 
 extern "C" mcx_status mcx_pass_timing(mcx_engine *e, int n, float *pass_ms, float *total_ms) {
   if (!e) return fail(nullptr, MCX_ERR_INVALID, "null engine");

@@ -16,6 +16,7 @@ struct Variant {
   int pot;
   bool mask;
   bool field;
+  bool per;  // every replica periodic in x, y and z with nx a multiple of 4 (no mask)
 };
 
 // What a pass launch does.

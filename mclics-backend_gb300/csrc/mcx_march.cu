@@ -64,7 +64,7 @@ __device__ __forceinline__ void load_opair_at(const March &m, int off, int offp,
 
 // One plane of the march: the pair at m.off with its z neighbours om (plane
 // below) and op (plane above; zp/zm: those bonds exist).
-template <int POT, bool MASK, bool FIELD, int MODE>
+template <int POT, bool MASK, bool FIELD, int MODE, bool PER>
 __device__ __forceinline__ void march_plane(const PassArgs &a, const RepDev &R, int c, const March &m,
                                             const OPair &om, const OPair &o0, const OPair &op, bool zp, bool zm,
                                             uint32_t seed, uint32_t stream, unsigned long long sw, float ang,
@@ -89,8 +89,10 @@ __device__ __forceinline__ void march_plane(const PassArgs &a, const RepDev &R, 
   float uA[3], uB[3];
   pair_uniforms(rw, uA, uB);
   auto wt = [&](float ee, uint8_t pp) { return MASK ? (ee != 0.f && pp != 0 ? 1.f : 0.f) : ee; };
-  const float exe = m.s ? m.ee1 : m.ee0;
-  const float erz[4] = {m.eyp, m.eym, zp ? 1.f : 0.f, zm ? 1.f : 0.f};
+  // PER: every bond exists (all axes periodic, pairs always complete)
+  const float exe = PER ? 1.f : (m.s ? m.ee1 : m.ee0);
+  const float erz[4] = {PER ? 1.f : m.eyp, PER ? 1.f : m.eym, PER || zp ? 1.f : 0.f, PER || zm ? 1.f : 0.f};
+  const bool hasB = PER || m.hasB;
   const OPair *rows4[4] = {&yp, &ym, &op, &om};
   const uint8_t lo = (uint8_t)(o0.pt & 0xFF), hi = (uint8_t)(o0.pt >> 8);
   float nb[6][3], w[6], e[6];
@@ -99,7 +101,7 @@ __device__ __forceinline__ void march_plane(const PassArgs &a, const RepDev &R, 
       nb[0][0] = o0.v[0].x; nb[0][1] = o0.v[1].x; nb[0][2] = o0.v[2].x; e[0] = 1.f; w[0] = wt(1.f, lo);
       nb[1][0] = exv[0]; nb[1][1] = exv[1]; nb[1][2] = exv[2]; e[1] = exe; w[1] = wt(exe, pex);
     } else {
-      if (m.hasB) {
+      if (hasB) {
         nb[0][0] = o0.v[0].y; nb[0][1] = o0.v[1].y; nb[0][2] = o0.v[2].y; e[0] = 1.f; w[0] = wt(1.f, hi);
       } else {
         nb[0][0] = exv[0]; nb[0][1] = exv[1]; nb[0][2] = exv[2]; e[0] = exe; w[0] = wt(exe, pex);
@@ -124,7 +126,7 @@ __device__ __forceinline__ void march_plane(const PassArgs &a, const RepDev &R, 
     acc += site_update<POT, MASK, FIELD, MODE>(R, a, c, ax.x, ay.x, az.x, nb, w, e, ps, sx, sy, sz, uA, ang, invT,
                                                0u, qs);
   }
-  if (m.hasB) {  // site B
+  if (hasB) {  // site B
     if (m.s == 0) {
       nb[0][0] = o0.v[0].y; nb[0][1] = o0.v[1].y; nb[0][2] = o0.v[2].y; e[0] = 1.f; w[0] = wt(1.f, hi);
       nb[1][0] = o0.v[0].x; nb[1][1] = o0.v[1].x; nb[1][2] = o0.v[2].x; e[1] = 1.f; w[1] = wt(1.f, lo);
@@ -163,7 +165,7 @@ constexpr int march_min_blocks() {
   return POT == POT_LL && !MASK ? (NT == 64 ? 9 : (NT == 128 ? 5 : 2)) : 1;
 }
 
-template <int POT, bool MASK, bool FIELD, int MODE, int NT>
+template <int POT, bool MASK, bool FIELD, int MODE, int NT, bool PER>
 __global__ void __launch_bounds__(NT, march_min_blocks<POT, MASK, NT>()) k_march(PassArgs a) {
   static_assert(MODE == MODE_SWEEP || MODE == MODE_SWEEP_MEASURE, "sweep modes only");
   const int4 u = a.units[blockIdx.x];
@@ -232,7 +234,7 @@ __global__ void __launch_bounds__(NT, march_min_blocks<POT, MASK, NT>()) k_march
       const bool zp = k + 1 < nz || zper;
       const int up = k + 1 < nz ? 1 : 1 - nz;
       load_opair_at<MASK>(m, m.off + up * m.dz, m.offp + up * m.dzp, zp, op);
-      march_plane<POT, MASK, FIELD, MODE>(a, R, c, m, om, o0, op, zp, zm, seed, stream, sw, ang, invT, acc, qs);
+      march_plane<POT, MASK, FIELD, MODE, PER>(a, R, c, m, om, o0, op, zp, zm, seed, stream, sw, ang, invT, acc, qs);
       om = o0;
       o0 = op;
       zm = true;
@@ -248,20 +250,27 @@ __global__ void __launch_bounds__(NT, march_min_blocks<POT, MASK, NT>()) k_march
 // ---------------------------------------------------------------------------
 // Launchers.
 // ---------------------------------------------------------------------------
-template <int POT, bool MASK, bool FIELD, int NT>
+template <int POT, bool MASK, bool FIELD, int NT, bool PER>
 static const void *march_fn(int mode) {
-  return mode == MODE_SWEEP_MEASURE ? (const void *)k_march<POT, MASK, FIELD, MODE_SWEEP_MEASURE, NT>
-                                    : (const void *)k_march<POT, MASK, FIELD, MODE_SWEEP, NT>;
+  return mode == MODE_SWEEP_MEASURE ? (const void *)k_march<POT, MASK, FIELD, MODE_SWEEP_MEASURE, NT, PER>
+                                    : (const void *)k_march<POT, MASK, FIELD, MODE_SWEEP, NT, PER>;
+}
+
+template <int POT, bool FIELD, int NT>
+static const void *march_fn_unmasked(const Variant &v, int mode) {
+  return v.per ? march_fn<POT, false, FIELD, NT, true>(mode) : march_fn<POT, false, FIELD, NT, false>(mode);
 }
 
 template <int NT>
 static const void *march_fn_v(const Variant &v, int mode) {
   if (v.pot == POT_LL) {
-    if (v.mask) return v.field ? march_fn<POT_LL, true, true, NT>(mode) : march_fn<POT_LL, true, false, NT>(mode);
-    return v.field ? march_fn<POT_LL, false, true, NT>(mode) : march_fn<POT_LL, false, false, NT>(mode);
+    if (v.mask)
+      return v.field ? march_fn<POT_LL, true, true, NT, false>(mode) : march_fn<POT_LL, true, false, NT, false>(mode);
+    return v.field ? march_fn_unmasked<POT_LL, true, NT>(v, mode) : march_fn_unmasked<POT_LL, false, NT>(v, mode);
   }
-  if (v.mask) return v.field ? march_fn<POT_GHRL, true, true, NT>(mode) : march_fn<POT_GHRL, true, false, NT>(mode);
-  return v.field ? march_fn<POT_GHRL, false, true, NT>(mode) : march_fn<POT_GHRL, false, false, NT>(mode);
+  if (v.mask)
+    return v.field ? march_fn<POT_GHRL, true, true, NT, false>(mode) : march_fn<POT_GHRL, true, false, NT, false>(mode);
+  return v.field ? march_fn_unmasked<POT_GHRL, true, NT>(v, mode) : march_fn_unmasked<POT_GHRL, false, NT>(v, mode);
 }
 
 static const void *march_kernel(const Variant &v, int mode, int nt) {

@@ -148,6 +148,7 @@ def lib() -> C.CDLL:
         L.mcx_stream.argtypes = [V]
         L.mcx_stream.restype = V
         L.mcx_pass_timing.argtypes = [V, I, C.POINTER(F), C.POINTER(F)]
+        L.mcx_sweep_timing.argtypes = [V, I, C.POINTER(F)]
         L.mcx_set_mlp.argtypes = [V, V, I]
         L.mcx_get_mlp.argtypes = [V, V]
         L.mcx_set_proposal.argtypes = [V, I]
