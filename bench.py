@@ -431,7 +431,9 @@ def main():
                    "l2": "flushed (256 MiB write) between steps outside the timed windows; the 25 MB lattice "
                          "stays L2-resident within a step",
                    "parallelism": (f"replicas x{ws} ranks" if ws > 1 else "one GPU") + f", {R} lattice(s) per engine",
-                   "pass_kernel": (f"z-march, {tuned[0]} threads x {tuned[1]} planes per CTA (autotuned)"
+                   "pass_kernel": ((f"z-march, {tuned[0]} threads x {tuned[1]} planes per CTA (autotuned)" if tuned[1] > 0
+                                    else f"z-march, {tuned[0]} threads x balanced chunks filling "
+                                         f"{max(1, -tuned[1])} wave(s) of resident CTAs (autotuned)")
                                    if args.proposal == "plain" else "learned-proposal pass (k_pass, BF16 MLP)"),
                    "S_E_last_step": [rows[-1][0], rows[-1][1], rows[-1][2]] if rows else None},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,

@@ -225,10 +225,13 @@ typedef enum { MCX_PASS_MARCH = 0, MCX_PASS_DIRECT = 1, MCX_PASS_STAGED = 2 } mc
 mcx_status mcx_set_pass(mcx_engine *eng, int kind);
 int mcx_get_pass(const mcx_engine *eng);
 /* The z-march pass's shape: CTA size (64, 128 or 256 threads, one site pair
- * each) and chunk depth (planes per CTA).  Default 128 x 8. */
+ * each) and chunk depth (planes per CTA; planes <= 0 cuts near-equal chunks
+ * so that the work units fill max(1, -planes) waves of the CTAs the GPU holds
+ * at once).  Default 128 x 8. */
 mcx_status mcx_set_march_shape(mcx_engine *eng, int block, int planes);
 /* Autotuner: times the z-march pass for block sizes {64, 128, 256} and chunk
- * depths {1, 2, 4, ..., 32} (up to the deepest lattice) on a scratch copy of
+ * depths {1, 2, 4, ..., 32} (up to the deepest lattice) and balanced chunks
+ * over 1 to 4 waves (planes 0, -2, -3, -4) on a scratch copy of
  * the engine's state (the state itself is untouched), keeps the fastest and
  * reports it (any output may be NULL).  Synchronous. */
 mcx_status mcx_autotune(mcx_engine *eng, int *block, int *planes, float *pass_us);

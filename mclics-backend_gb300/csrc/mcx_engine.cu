@@ -71,6 +71,7 @@ struct mcx_engine {
   // z-march pass (the default sweep pass of the plain proposal)
   bool march = true;
   int march_nt = 128, march_k = 8;
+  bool pdl = true;  // programmatic dependent launch of the z-march passes
   std::vector<int4> units;
   int4 *d_units = nullptr;
   long long dir_total = 0;  // floats of d_dir
@@ -229,18 +230,47 @@ static void effective_bounds(mcx_replica_desc &d) {
 // Work units of the z-march pass: per replica, blocks of march_nt pairs of a
 // plane times chunks of march_k planes, chunk-major so that the CTAs resident
 // together work on neighbouring planes.
+//
+// march_k > 0 fixes the chunk depth.  march_k <= 0 balances the chunks
+// against the CTAs the GPU holds at once (SMs x resident CTAs of the kernel):
+// the column blocks of all replicas are cut into chunks of near-equal depth
+// (sizes differ by at most one plane) so that the units fill max(1, -march_k)
+// waves, which keeps the last wave from running mostly idle.
 static void plan_march(mcx_engine *e) {
   e->units.clear();
+  const int nt = e->march_nt;
+  double avg = 0.0;  // balanced: planes per unit
+  if (e->march_k <= 0) {
+    int dev = 0, nsm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    const long long slots = (long long)std::max(1, nsm) * std::max(1, march_blocks_per_sm(e->var, MODE_SWEEP, nt)) *
+                            std::max(1, -e->march_k);
+    long long work = 0;
+    for (const RepDev &R : e->rep) work += (long long)((R.hp * R.ny + nt - 1) / nt) * R.nz;
+    avg = std::max(1.0, (double)work / (double)slots);
+  }
   for (int r = 0; r < e->nrep; r++) {
     RepDev &R = e->rep[r];
     const int npp = R.hp * R.ny;
-    const int K = std::max(1, std::min(e->march_k, R.nz));
     R.mcta = 0;
-    for (int k0 = 0; k0 < R.nz; k0 += K)
-      for (int p0 = 0; p0 < npp; p0 += e->march_nt) {
-        e->units.push_back(make_int4(r, p0, k0, std::min(K, R.nz - k0)));
-        R.mcta++;
+    if (e->march_k > 0) {
+      const int K = std::min(e->march_k, R.nz);
+      for (int k0 = 0; k0 < R.nz; k0 += K)
+        for (int p0 = 0; p0 < npp; p0 += nt) {
+          e->units.push_back(make_int4(r, p0, k0, std::min(K, R.nz - k0)));
+          R.mcta++;
+        }
+    } else {
+      const int chunks = std::max(1, std::min(R.nz, (int)std::lround(R.nz / avg)));
+      for (int q = 0; q < chunks; q++) {
+        const int k0 = (int)((long long)q * R.nz / chunks), k1 = (int)((long long)(q + 1) * R.nz / chunks);
+        for (int p0 = 0; p0 < npp; p0 += nt) {
+          e->units.push_back(make_int4(r, p0, k0, k1 - k0));
+          R.mcta++;
+        }
       }
+    }
   }
 }
 
@@ -335,6 +365,8 @@ extern "C" mcx_status mcx_create(int n, const mcx_replica_desc *descs, mcx_engin
     if (nt && march_block_ok(atoi(nt))) e->march_nt = atoi(nt);
     if (kk && atoi(kk) > 0) e->march_k = atoi(kk);
     if (mo && atoi(mo) == 0) e->march = false;
+    const char *pd = getenv("MCX_PDL");
+    if (pd && atoi(pd) == 0) e->pdl = false;
     plan_march(e);
   }
   {
@@ -638,7 +670,7 @@ static void launch_sweep_pass(mcx_engine *e, PassArgs &pa, int colour, bool meas
   const int mode = measure ? MODE_SWEEP_MEASURE : MODE_SWEEP;
   if (e->proposal == MCX_PROPOSAL_VMF_MLP) launch_pass_learned(e->var, mode, pa, e->lgrid[mode], e->stream);
   else if (e->staged) launch_tpass(e->var, mode, pa, e->grid[measure ? 1 : 0], e->stream);
-  else if (e->march) launch_march(e->var, mode, pa, e->march_nt, e->stream);
+  else if (e->march) launch_march(e->var, mode, pa, e->march_nt, e->pdl, e->stream);
   else launch_pass(e->var, mode, pa, e->pgrid[mode], e->stream);
 }
 
@@ -772,7 +804,7 @@ static mcx_status apply_march_shape(mcx_engine *e, int nt, int k) {
 
 extern "C" mcx_status mcx_set_march_shape(mcx_engine *e, int block, int planes) {
   if (!e) return fail(nullptr, MCX_ERR_INVALID, "null engine");
-  if (!march_block_ok(block) || planes < 1) return fail(e, MCX_ERR_INVALID, "z-march shape %d threads x %d planes", block, planes);
+  if (!march_block_ok(block) || planes < -8) return fail(e, MCX_ERR_INVALID, "z-march shape %d threads x %d planes", block, planes);
   CK(e, cudaStreamSynchronize(e->stream));
   return apply_march_shape(e, block, planes);
 }
@@ -811,9 +843,11 @@ extern "C" mcx_status mcx_autotune(mcx_engine *e, int *block, int *planes, float
   CKA(cudaMemcpyAsync(d_st, e->d_st, sizeof(RepState) * e->nrep, cudaMemcpyDeviceToDevice, e->stream));
   {
     const int nts[3] = {64, 128, 256};
+    const int ks[10] = {1, 2, 4, 8, 16, 32, 0, -2, -3, -4};  // fixed depths, then balanced over 1..4 waves
     for (int a = 0; a < 3; a++)
-      for (int k = 1; k <= 32; k *= 2) {
-        if (k > maxnz && k > 1) break;
+      for (int ki = 0; ki < 10; ki++) {
+        const int k = ks[ki];
+        if (k > maxnz && k > 1) continue;
         if ((st = apply_march_shape(e, nts[a], k))) goto done;
         PassArgs pa = pass_args(e);
         pa.dir = d_dir;
@@ -824,13 +858,13 @@ extern "C" mcx_status mcx_autotune(mcx_engine *e, int *block, int *planes, float
         for (int w = 0; w < 2; w++)
           for (int c = 0; c < 2; c++) {
             pa.colour = c;
-            launch_march(e->var, MODE_SWEEP, pa, nts[a], e->stream);
+            launch_march(e->var, MODE_SWEEP, pa, nts[a], e->pdl, e->stream);
           }
         CKA(cudaEventRecord(t0, e->stream));
         for (int q = 0; q < reps; q++)
           for (int c = 0; c < 2; c++) {
             pa.colour = c;
-            launch_march(e->var, MODE_SWEEP, pa, nts[a], e->stream);
+            launch_march(e->var, MODE_SWEEP, pa, nts[a], e->pdl, e->stream);
           }
         CKA(cudaEventRecord(t1, e->stream));
         CKA(cudaGetLastError());

@@ -70,9 +70,12 @@ struct FlushArgs {
 // The direct pass over a.map with `nblocks` persistent CTAs.
 void launch_pass(const Variant &v, int mode, const PassArgs &a, int nblocks, cudaStream_t st);
 int pass_blocks_per_sm(const Variant &v, int mode);
-// The z-march pass (mcx_march.cu): one CTA of nt threads per unit of a.units.
-void launch_march(const Variant &v, int mode, const PassArgs &a, int nt, cudaStream_t st);
+// The z-march pass (mcx_march.cu): one CTA of nt threads per unit of a.units;
+// pdl lets the launch overlap the previous grid's tail (programmatic
+// dependent launch; the kernel waits for it before touching shared state).
+void launch_march(const Variant &v, int mode, const PassArgs &a, int nt, bool pdl, cudaStream_t st);
 bool march_block_ok(int nt);
+int march_blocks_per_sm(const Variant &v, int mode, int nt);
 // The direct pass with the learned proposal (mcx_learned.cu).
 void launch_pass_learned(const Variant &v, int mode, const PassArgs &a, int nblocks, cudaStream_t st);
 int pass_learned_blocks_per_sm(const Variant &v, int mode);

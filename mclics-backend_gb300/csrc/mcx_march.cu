@@ -26,6 +26,12 @@ namespace mcx {
 
 __device__ __forceinline__ float2 ldg2(const float *p) { return __ldg(reinterpret_cast<const float2 *>(p)); }
 
+// Programmatic dependent launch: wait until the preceding grid on the stream
+// has completed and its memory is visible (returns at once when the launch
+// had no programmatic dependency), and let the following grid be scheduled.
+__device__ __forceinline__ void grid_dependency_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void grid_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;" :::); }
+
 // Opposite-colour pair of one row: 3 components (and point types).
 struct OPair {
   float2 v[3];
@@ -218,6 +224,10 @@ __global__ void __launch_bounds__(NT, march_min_blocks<POT, MASK, NT>()) k_march
     m.dpid = (uint32_t)ny * (uint32_t)R.hp;
     m.s = (c + j + kb) & 1;
     const uint32_t seed = R.seed, stream = R.stream;
+    // everything above depends only on constants; the state and the
+    // directors may still be written by the previous pass (programmatic
+    // dependent launch lets this grid start while that one drains)
+    grid_dependency_wait();
     const unsigned long long sw = S->sweep;
     const float ang = S->ang_var, invT = 1.0f / S->T;
     // the z pipeline: opposite pairs of this column at planes k-1, k, k+1
@@ -244,6 +254,8 @@ __global__ void __launch_bounds__(NT, march_min_blocks<POT, MASK, NT>()) k_march
       m.s ^= 1;
     }
   }
+  grid_dependency_wait();    // threads without a pair reach here without having waited
+  grid_launch_dependents();  // the next pass may start its set-up now
   flush_replica<NT, MODE>(a, r, 1, (unsigned)R.mcta, acc, qs, MASK);
 }
 
@@ -283,10 +295,26 @@ static const void *march_kernel(const Variant &v, int mode, int nt) {
 
 bool march_block_ok(int nt) { return nt == 64 || nt == 128 || nt == 256; }
 
-void launch_march(const Variant &v, int mode, const PassArgs &a, int nt, cudaStream_t st) {
+int march_blocks_per_sm(const Variant &v, int mode, int nt) {
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, march_kernel(v, mode, nt), nt, 0) != cudaSuccess) return 0;
+  return n;
+}
+
+void launch_march(const Variant &v, int mode, const PassArgs &a, int nt, bool pdl, cudaStream_t st) {
   PassArgs args = a;
   void *params[] = {&args};
-  cudaLaunchKernel(march_kernel(v, mode, nt), dim3(a.nunits), dim3(nt), params, 0, st);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(a.nunits);
+  cfg.blockDim = dim3(nt);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = pdl ? 1 : 0;
+  cudaLaunchKernelExC(&cfg, march_kernel(v, mode, nt), params);
 }
 
 }  // namespace mcx

@@ -238,8 +238,8 @@ def test_errors_are_status_codes():
             e.set_field(1.0)
 
 
-KERNELS = [("march", 128, 8), ("march", 64, 1), ("march", 256, 32), ("march", 128, 3), ("direct", 0, 0),
-           ("staged", 0, 0)]
+KERNELS = [("march", 128, 8), ("march", 64, 1), ("march", 256, 32), ("march", 128, 3), ("march", 128, 0),
+           ("march", 64, -3), ("direct", 0, 0), ("staged", 0, 0)]
 
 
 def _run_kernel(descs, setup, kind, block, planes, sweeps=19):
@@ -304,7 +304,7 @@ def test_pass_kernels_agree_on_uneven_batch():
             eng.set_state(r, random_state(m, np.ones(m.n, np.int32), np.random.default_rng(r)))
 
     ref = _run_kernel(descs, setup, "direct", 0, 0, sweeps=21)
-    for kind, block, planes in KERNELS[:4]:
+    for kind, block, planes in KERNELS[:6]:
         _assert_same(ref, _run_kernel(descs, setup, kind, block, planes, sweeps=21))
 
 
@@ -316,7 +316,7 @@ def test_autotune_keeps_state_and_results():
         a.set_state(0, ni0)
         b.set_state(0, ni0)
         block, planes, us = a.autotune()
-        assert block in (64, 128, 256) and 1 <= planes <= 32 and us > 0
+        assert block in (64, 128, 256) and -4 <= planes <= 32 and us > 0
         assert np.array_equal(a.get_state(0), ni0)
         assert a.stats(0)[mcx.ST_SWEEP_INDEX] == 0
         a.sweep(40, measure=True)
