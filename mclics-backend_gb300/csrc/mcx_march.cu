@@ -164,11 +164,16 @@ __device__ __forceinline__ void march_plane(const PassArgs &a, const RepDev &R, 
 }
 
 // Resident CTAs per SM the compiler is asked for (measured best): the
-// unmasked Lebwohl-Lasher pass at about 100-113 registers per thread; the
-// GHRL and masked variants unconstrained (they spill under a cap).
+// unmasked Lebwohl-Lasher pass at about 96-113 registers per thread; the GHRL
+// and masked variants at 128 (they spill a little there, and still run 1.5x
+// faster than unconstrained at 160-206 registers, from the doubled occupancy).
+#ifndef MCX_MARCH_MASK_REGS
+#define MCX_MARCH_MASK_REGS 128
+#endif
 template <int POT, bool MASK, int NT>
 constexpr int march_min_blocks() {
-  return POT == POT_LL && !MASK ? (NT == 64 ? 9 : (NT == 128 ? 5 : 2)) : 1;
+  return POT == POT_LL && !MASK ? (NT == 64 ? 9 : (NT == 128 ? 5 : 2))
+                                : (MCX_MARCH_MASK_REGS > 0 ? 65536 / (NT * MCX_MARCH_MASK_REGS) : 1);
 }
 
 template <int POT, bool MASK, bool FIELD, int MODE, int NT, bool PER>
