@@ -219,9 +219,12 @@ int mcx_get_staged(const mcx_engine *eng);
  *                    the z neighbours in registers;
  *   MCX_PASS_DIRECT  persistent CTAs, each pair's neighbourhood loaded by
  *                    cp.async into shared memory;
- *   MCX_PASS_STAGED  the staged TMA pass above (mcx_set_staged).
+ *   MCX_PASS_STAGED  the staged TMA pass above (mcx_set_staged);
+ *   MCX_PASS_MARCH_TMA  the z-march with each plane's rows brought into
+ *                    shared memory by bulk copies one plane ahead (unmasked
+ *                    batches only).
  * No counterpart in the reference. */
-typedef enum { MCX_PASS_MARCH = 0, MCX_PASS_DIRECT = 1, MCX_PASS_STAGED = 2 } mcx_pass_kind;
+typedef enum { MCX_PASS_MARCH = 0, MCX_PASS_DIRECT = 1, MCX_PASS_STAGED = 2, MCX_PASS_MARCH_TMA = 3 } mcx_pass_kind;
 mcx_status mcx_set_pass(mcx_engine *eng, int kind);
 int mcx_get_pass(const mcx_engine *eng);
 /* The z-march pass's shape: CTA size (64, 128 or 256 threads, one site pair
@@ -229,7 +232,8 @@ int mcx_get_pass(const mcx_engine *eng);
  * so that the work units fill max(1, -planes) waves of the CTAs the GPU holds
  * at once).  Default 128 x 8. */
 mcx_status mcx_set_march_shape(mcx_engine *eng, int block, int planes);
-/* Autotuner: times the z-march pass for block sizes {64, 128, 256} and chunk
+/* Autotuner: times the z-march pass (register and, for unmasked batches,
+ * TMA-staged forms) for block sizes {64, 128, 256} and chunk
  * depths {1, 2, 4, ..., 32} (up to the deepest lattice) and balanced chunks
  * over 1 to 4 waves (planes 0, -2, -3, -4) on a scratch copy of
  * the engine's state (the state itself is untouched), keeps the fastest and

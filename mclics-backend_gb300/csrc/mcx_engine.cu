@@ -72,6 +72,8 @@ struct mcx_engine {
   bool march = true;
   int march_nt = 128, march_k = 8;
   bool pdl = true;  // programmatic dependent launch of the z-march passes
+  bool tmarch = false;  // the z-march with rows staged by bulk copies (unmasked lattices)
+  int tm_o = 0, tm_a = 0;  // its shared-memory slot sizes (floats)
   std::vector<int4> units;
   int4 *d_units = nullptr;
   long long dir_total = 0;  // floats of d_dir
@@ -88,6 +90,7 @@ struct mcx_engine {
 
 static void drop_graphs(mcx_engine *e);
 static PassArgs pass_args(mcx_engine *e);
+static bool use_tmarch(mcx_engine *e, bool on);
 
 static mcx_status fail(mcx_engine *e, mcx_status st, const char *fmt, ...) {
   char buf[512];
@@ -262,7 +265,8 @@ static void plan_march(mcx_engine *e) {
           R.mcta++;
         }
     } else {
-      const int chunks = std::max(1, std::min(R.nz, (int)std::lround(R.nz / avg)));
+      // rounded down, so that the units never exceed the waves asked for
+      const int chunks = std::max(1, std::min(R.nz, (int)std::floor(R.nz / avg)));
       for (int q = 0; q < chunks; q++) {
         const int k0 = (int)((long long)q * R.nz / chunks), k1 = (int)((long long)(q + 1) * R.nz / chunks);
         for (int p0 = 0; p0 < npp; p0 += nt) {
@@ -661,6 +665,8 @@ static PassArgs pass_args(mcx_engine *e) {
   pa.err = e->d_err;
   pa.units = e->d_units;
   pa.nunits = (int)e->units.size();
+  pa.tm_o = e->tm_o;
+  pa.tm_a = e->tm_a;
   return pa;
 }
 
@@ -670,6 +676,7 @@ static void launch_sweep_pass(mcx_engine *e, PassArgs &pa, int colour, bool meas
   const int mode = measure ? MODE_SWEEP_MEASURE : MODE_SWEEP;
   if (e->proposal == MCX_PROPOSAL_VMF_MLP) launch_pass_learned(e->var, mode, pa, e->lgrid[mode], e->stream);
   else if (e->staged) launch_tpass(e->var, mode, pa, e->grid[measure ? 1 : 0], e->stream);
+  else if (e->march && e->tmarch) launch_tmarch(e->var, mode, pa, e->march_nt, e->pdl, e->stream);
   else if (e->march) launch_march(e->var, mode, pa, e->march_nt, e->pdl, e->stream);
   else launch_pass(e->var, mode, pa, e->pgrid[mode], e->stream);
 }
@@ -758,12 +765,15 @@ extern "C" mcx_status mcx_sync(mcx_engine *e) {
 
 extern "C" mcx_status mcx_set_pass(mcx_engine *e, int kind) {
   if (!e) return fail(nullptr, MCX_ERR_INVALID, "null engine");
-  if (kind < MCX_PASS_MARCH || kind > MCX_PASS_STAGED) return fail(e, MCX_ERR_INVALID, "unknown pass kernel %d", kind);
+  if (kind < MCX_PASS_MARCH || kind > MCX_PASS_MARCH_TMA) return fail(e, MCX_ERR_INVALID, "unknown pass kernel %d", kind);
   if (kind == MCX_PASS_STAGED && !e->can_stage)
     return fail(e, MCX_ERR_UNSUPPORTED, "a replica's rows do not fit the staged pass's shared memory");
   CK(e, cudaStreamSynchronize(e->stream));
+  if (kind == MCX_PASS_MARCH_TMA && !use_tmarch(e, true))
+    return fail(e, MCX_ERR_UNSUPPORTED, "the TMA-staged z-march needs an unmasked batch whose rows fit in shared memory");
+  if (kind != MCX_PASS_MARCH_TMA) e->tmarch = false;
   e->staged = kind == MCX_PASS_STAGED;
-  e->march = kind == MCX_PASS_MARCH;
+  e->march = kind == MCX_PASS_MARCH || kind == MCX_PASS_MARCH_TMA;
   for (int m = 0; m < 2; m++)
     if (e->graph[m]) {
       cudaGraphExecDestroy(e->graph[m]);
@@ -774,7 +784,7 @@ extern "C" mcx_status mcx_set_pass(mcx_engine *e, int kind) {
 
 extern "C" int mcx_get_pass(const mcx_engine *e) {
   if (!e) return -1;
-  return e->staged ? MCX_PASS_STAGED : (e->march ? MCX_PASS_MARCH : MCX_PASS_DIRECT);
+  return e->staged ? MCX_PASS_STAGED : (e->march ? (e->tmarch ? MCX_PASS_MARCH_TMA : MCX_PASS_MARCH) : MCX_PASS_DIRECT);
 }
 
 extern "C" mcx_status mcx_set_staged(mcx_engine *e, int on) {
@@ -785,11 +795,39 @@ extern "C" int mcx_get_staged(const mcx_engine *e) { return e && e->staged ? 1 :
 
 // Re-plans the z-march units for a block size and chunk depth and uploads
 // them with the replicas' CTA counts.
+// Shared-memory slots of the TMA-staged z-march for the current units: an O
+// slot holds 3 components x (rows spanned + 2) rows, an A slot 3 x rows.
+static void plan_tmarch_slots(mcx_engine *e) {
+  long long o = 0, a = 0;
+  for (const int4 &u : e->units) {
+    const RepDev &R = e->rep[u.x];
+    const int pend = std::min(u.y + e->march_nt, R.hp * R.ny);
+    const int nrA = (pend - 1) / R.hp - u.y / R.hp + 1;
+    o = std::max(o, 3LL * (nrA + 2) * R.hs);
+    a = std::max(a, 3LL * nrA * R.hs);
+  }
+  e->tm_o = (int)align_up(o, 32);
+  e->tm_a = (int)align_up(a, 32);
+}
+
+// Selects the TMA-staged form of the z-march when it can run (unmasked
+// lattices whose slots fit in shared memory).
+static bool use_tmarch(mcx_engine *e, bool on) {
+  e->tmarch = false;
+  if (!on || e->var.mask) return false;
+  plan_tmarch_slots(e);
+  const long long bytes = (4LL * e->tm_o + 2LL * e->tm_a) * 4;
+  if (bytes > 200 * 1024) return false;
+  e->tmarch = tmarch_prepare(e->var, e->march_nt, (int)bytes);
+  return e->tmarch;
+}
+
 static mcx_status apply_march_shape(mcx_engine *e, int nt, int k) {
   e->march_nt = nt;
   e->march_k = k;
   const size_t before = e->units.size();
   plan_march(e);
+  if (e->tmarch) use_tmarch(e, true);
   if (e->units.size() > before || !e->d_units) {
     cudaFree(e->d_units);
     e->d_units = nullptr;
@@ -823,7 +861,7 @@ extern "C" mcx_status mcx_autotune(mcx_engine *e, int *block, int *planes, float
   const size_t ring_n = (size_t)e->nrep * (e->ring_cap + 1) * kLanes * kQ;
   cudaEvent_t t0, t1;
   mcx_status st = MCX_OK;
-  int best_nt = e->march_nt, best_k = e->march_k;
+  int best_nt = e->march_nt, best_k = e->march_k, best_tma = e->tmarch ? 1 : 0;
   float best = 1e30f;
 #define CKA(call)                                                                                    \
   do {                                                                                               \
@@ -844,11 +882,14 @@ extern "C" mcx_status mcx_autotune(mcx_engine *e, int *block, int *planes, float
   {
     const int nts[3] = {64, 128, 256};
     const int ks[10] = {1, 2, 4, 8, 16, 32, 0, -2, -3, -4};  // fixed depths, then balanced over 1..4 waves
+    for (int tma = 0; tma < 2; tma++)
     for (int a = 0; a < 3; a++)
       for (int ki = 0; ki < 10; ki++) {
         const int k = ks[ki];
         if (k > maxnz && k > 1) continue;
+        e->tmarch = tma != 0;
         if ((st = apply_march_shape(e, nts[a], k))) goto done;
+        if (tma && !e->tmarch) continue;  // the staged form cannot run this batch or shape
         PassArgs pa = pass_args(e);
         pa.dir = d_dir;
         pa.st = d_st;
@@ -858,13 +899,15 @@ extern "C" mcx_status mcx_autotune(mcx_engine *e, int *block, int *planes, float
         for (int w = 0; w < 2; w++)
           for (int c = 0; c < 2; c++) {
             pa.colour = c;
-            launch_march(e->var, MODE_SWEEP, pa, nts[a], e->pdl, e->stream);
+            if (tma) launch_tmarch(e->var, MODE_SWEEP, pa, nts[a], e->pdl, e->stream);
+            else launch_march(e->var, MODE_SWEEP, pa, nts[a], e->pdl, e->stream);
           }
         CKA(cudaEventRecord(t0, e->stream));
         for (int q = 0; q < reps; q++)
           for (int c = 0; c < 2; c++) {
             pa.colour = c;
-            launch_march(e->var, MODE_SWEEP, pa, nts[a], e->pdl, e->stream);
+            if (tma) launch_tmarch(e->var, MODE_SWEEP, pa, nts[a], e->pdl, e->stream);
+            else launch_march(e->var, MODE_SWEEP, pa, nts[a], e->pdl, e->stream);
           }
         CKA(cudaEventRecord(t1, e->stream));
         CKA(cudaGetLastError());
@@ -877,9 +920,11 @@ extern "C" mcx_status mcx_autotune(mcx_engine *e, int *block, int *planes, float
           best = us;
           best_nt = nts[a];
           best_k = k;
+          best_tma = tma;
         }
       }
   }
+  e->tmarch = best_tma != 0;
   st = apply_march_shape(e, best_nt, best_k);
 done:
 #undef CKA

@@ -54,6 +54,8 @@ struct PassArgs {
   // z-march pass: (replica, first pair of the plane, first plane, planes)
   const int4 *units;
   int nunits;
+  // TMA-staged z-march: floats per O slot and per A slot of shared memory
+  int tm_o, tm_a;
 };
 
 struct FlushArgs {
@@ -75,6 +77,11 @@ int pass_blocks_per_sm(const Variant &v, int mode);
 // dependent launch; the kernel waits for it before touching shared state).
 void launch_march(const Variant &v, int mode, const PassArgs &a, int nt, bool pdl, cudaStream_t st);
 bool march_block_ok(int nt);
+// The z-march with its rows staged in shared memory by bulk copies (unmasked
+// lattices): prepare (shared-memory attribute, residency) once per shape.
+bool tmarch_prepare(const Variant &v, int nt, int smem_bytes);
+int tmarch_smem_bytes(const PassArgs &a);
+void launch_tmarch(const Variant &v, int mode, const PassArgs &a, int nt, bool pdl, cudaStream_t st);
 int march_blocks_per_sm(const Variant &v, int mode, int nt);
 // The direct pass with the learned proposal (mcx_learned.cu).
 void launch_pass_learned(const Variant &v, int mode, const PassArgs &a, int nblocks, cudaStream_t st);

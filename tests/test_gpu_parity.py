@@ -239,21 +239,23 @@ def test_errors_are_status_codes():
 
 
 KERNELS = [("march", 128, 8), ("march", 64, 1), ("march", 256, 32), ("march", 128, 3), ("march", 128, 0),
-           ("march", 64, -3), ("direct", 0, 0), ("staged", 0, 0)]
+           ("march", 64, -3), ("march_tma", 128, 8), ("march_tma", 256, 0), ("march_tma", 64, 3), ("direct", 0, 0),
+           ("staged", 0, 0)]
 
 
 def _run_kernel(descs, setup, kind, block, planes, sweeps=19):
     with mcx.Engine(descs) as eng:
-        if kind == "staged":
+        if kind in ("staged", "march_tma"):
             try:
-                eng.pass_kind = "staged"
+                eng.pass_kind = kind  # not every batch fits these kernels
             except mcx.McxError:
                 return None
         else:
             eng.pass_kind = kind
         assert eng.pass_kind == kind
-        if kind == "march":
+        if kind.startswith("march"):
             eng.set_march_shape(block, planes)
+            assert eng.pass_kind == kind
         setup(eng)
         eng.sweep(sweeps, measure=True)
         return [(eng.get_state(r), eng.stats(r)) for r in range(len(descs))]
@@ -304,7 +306,7 @@ def test_pass_kernels_agree_on_uneven_batch():
             eng.set_state(r, random_state(m, np.ones(m.n, np.int32), np.random.default_rng(r)))
 
     ref = _run_kernel(descs, setup, "direct", 0, 0, sweeps=21)
-    for kind, block, planes in KERNELS[:6]:
+    for kind, block, planes in KERNELS[:9]:
         _assert_same(ref, _run_kernel(descs, setup, kind, block, planes, sweeps=21))
 
 
