@@ -361,6 +361,35 @@ mcx_status mcx_check_file(const char *param_file, mcx_replica_desc *desc);
 mcx_status mcx_measure_noalloc(const mcx_replica_desc *desc, const float *d_ni_aos, const int *d_pt,
                                const float *d_ns_aos, double *d_out, void *stream);
 
+/* Local order parameter of every site of a replica (lattice_order_parameter,
+ * src/parameter_order.cpp:62-113, as the snapshot writer print_n,
+ * src/io.cpp:50-80, reports it): the largest eigenvalue of Q over the site and
+ * its existing active neighbours; NaN at inactive sites.  S: one float per
+ * site, natural order.  Computed on the GPU. */
+mcx_status mcx_local_order(mcx_engine *eng, int replica, float *S);
+
+/* Checkpoint (no counterpart in the reference): every replica's descriptor,
+ * directors, mask, temperature, step size, sweep and measured-sweep counters
+ * (the Philox counters: a loaded engine continues the saved trajectory bit
+ * for bit), running sums, and the network weights and proposal when set.  The
+ * measured-sweep series and the training optimiser state are not saved.
+ * mcx_load needs an engine of the same replica count, sizes, geometries,
+ * potentials and bounds. */
+mcx_status mcx_save(mcx_engine *eng, const char *path);
+mcx_status mcx_load(mcx_engine *eng, const char *path);
+
+/* Replica exchange (parallel tempering; no counterpart in the reference):
+ * for each pair (pairs[2i], pairs[2i+1]) of replicas with the same
+ * Hamiltonian (descriptors equal except T, step size and RNG keys), swap
+ * their temperatures and step sizes with probability
+ * min(1, exp((1/Ta - 1/Tb)(Ha - Hb))), H = E * sites the total energy of the
+ * current states; the uniform is Philox4x32-10 of (i, round, TAG 4) with key
+ * (seed, 0).  accepted (n ints, may be NULL) receives the decisions.  The
+ * running sums stay with the replica (reset them after an exchange to gather
+ * statistics per temperature). */
+mcx_status mcx_exchange(mcx_engine *eng, int n_pairs, const int *pairs, unsigned int seed, unsigned long long round,
+                        int *accepted);
+
 /* ./mc_sim <param_file> (src/main.cpp:63-83): reads the reference's parameter
  * file (src/io.cpp:81-253), runs the selected mode on the GPU and writes
  * po.dat and director_field_*.csv into out_dir (NULL: current directory). */

@@ -33,7 +33,7 @@ enum : int {
 };
 // Philox counter word 3: which stream of uniforms.
 // The pass colour is or-ed into the low bit.
-enum : uint32_t { TAG_PLAIN = 0u, TAG_VMF = 2u, TAG_IC = 0x1C000000u };
+enum : uint32_t { TAG_PLAIN = 0u, TAG_VMF = 2u, TAG_PT = 4u, TAG_IC = 0x1C000000u };
 
 // Per-replica constants, resident in device memory (read-only in kernels).
 struct RepDev {

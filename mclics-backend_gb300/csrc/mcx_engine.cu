@@ -1148,6 +1148,197 @@ extern "C" mcx_status mcx_train_mlp(mcx_engine *e, const mcx_train_config *cfg, 
   return MCX_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Snapshots, checkpoints, replica exchange.
+// ---------------------------------------------------------------------------
+extern "C" mcx_status mcx_local_order(mcx_engine *e, int r, float *S) {
+  if (mcx_status st = check_rep(e, r)) return st;
+  if (!S) return fail(e, MCX_ERR_INVALID, "mcx_local_order: null output");
+  const RepDev &R = e->rep[r];
+  launch_local_order(R, e->d_dir, e->d_pt, e->d_stage, e->stream);
+  e->launches++;
+  CKL(e);
+  CK(e, cudaMemcpyAsync(S, e->d_stage, sizeof(float) * R.ntot, cudaMemcpyDeviceToHost, e->stream));
+  CK(e, cudaStreamSynchronize(e->stream));
+  return MCX_OK;
+}
+
+namespace {
+const char kCkptMagic[8] = {'M', 'C', 'X', 'C', 'K', 'P', 'T', '1'};
+struct CkptState {
+  float T, ang_var;
+  unsigned long long sweep, meas;
+  unsigned int frozen, pad;
+};
+struct FileCloser {
+  FILE *f;
+  ~FileCloser() {
+    if (f) fclose(f);
+  }
+};
+}  // namespace
+
+extern "C" mcx_status mcx_save(mcx_engine *e, const char *path) {
+  if (!e || !path) return fail(e, MCX_ERR_INVALID, "mcx_save: null argument");
+  if (mcx_status st = flush(e)) return st;
+  CK(e, cudaStreamSynchronize(e->stream));
+  FileCloser fc{fopen(path, "wb")};
+  if (!fc.f) return fail(e, MCX_ERR_IO, "mcx_save: cannot open %s", path);
+  std::vector<RepState> st(e->nrep);
+  std::vector<double> stats((size_t)kStats * e->nrep);
+  CK(e, cudaMemcpy(st.data(), e->d_st, sizeof(RepState) * e->nrep, cudaMemcpyDeviceToHost));
+  CK(e, cudaMemcpy(stats.data(), e->d_stats, sizeof(double) * stats.size(), cudaMemcpyDeviceToHost));
+  const uint32_t hdr[4] = {1u, (uint32_t)e->nrep, (uint32_t)sizeof(mcx_replica_desc), e->mlp.empty() ? 0u : 1u};
+  bool ok = fwrite(kCkptMagic, 1, 8, fc.f) == 8 && fwrite(hdr, sizeof hdr, 1, fc.f) == 1;
+  for (int r = 0; r < e->nrep && ok; r++) {
+    const RepDev &R = e->rep[r];
+    CkptState cs{st[r].T, st[r].ang_var, st[r].sweep, st[r].meas, st[r].frozen, 0u};
+    std::vector<float> ni(3 * (size_t)R.ntot);
+    if (mcx_status s2 = mcx_get_state(e, r, ni.data())) return s2;
+    ok = fwrite(&e->desc[r], sizeof(mcx_replica_desc), 1, fc.f) == 1 && fwrite(&cs, sizeof cs, 1, fc.f) == 1 &&
+         fwrite(stats.data() + (size_t)kStats * r, sizeof(double), kStats, fc.f) == (size_t)kStats &&
+         fwrite(ni.data(), sizeof(float), ni.size(), fc.f) == ni.size();
+    if (ok && e->var.mask) {
+      std::vector<int> pt(R.ntot);
+      std::vector<float> ns(3 * (size_t)R.ntot);
+      if (mcx_status s2 = mcx_get_mask(e, r, pt.data(), ns.data())) return s2;
+      ok = fwrite(pt.data(), sizeof(int), pt.size(), fc.f) == pt.size() &&
+           fwrite(ns.data(), sizeof(float), ns.size(), fc.f) == ns.size();
+    }
+  }
+  if (ok && !e->mlp.empty()) {
+    const int32_t prop = e->proposal;
+    ok = fwrite(&prop, sizeof prop, 1, fc.f) == 1 && fwrite(e->mlp.data(), sizeof(float), e->mlp.size(), fc.f) == e->mlp.size();
+  }
+  if (!ok) return fail(e, MCX_ERR_IO, "mcx_save: write to %s failed", path);
+  return MCX_OK;
+}
+
+extern "C" mcx_status mcx_load(mcx_engine *e, const char *path) {
+  if (!e || !path) return fail(e, MCX_ERR_INVALID, "mcx_load: null argument");
+  FileCloser fc{fopen(path, "rb")};
+  if (!fc.f) return fail(e, MCX_ERR_IO, "mcx_load: cannot open %s", path);
+  char magic[8];
+  uint32_t hdr[4];
+  if (fread(magic, 1, 8, fc.f) != 8 || memcmp(magic, kCkptMagic, 8) != 0 || fread(hdr, sizeof hdr, 1, fc.f) != 1)
+    return fail(e, MCX_ERR_PARSE, "mcx_load: %s is not an engine checkpoint", path);
+  if (hdr[0] != 1u || hdr[2] != sizeof(mcx_replica_desc))
+    return fail(e, MCX_ERR_PARSE, "mcx_load: checkpoint version %u / descriptor size %u not supported", hdr[0], hdr[2]);
+  if ((int)hdr[1] != e->nrep)
+    return fail(e, MCX_ERR_INVALID, "mcx_load: checkpoint holds %u replicas, the engine %d", hdr[1], e->nrep);
+  if (mcx_status st = flush(e)) return st;
+  CK(e, cudaStreamSynchronize(e->stream));
+  std::vector<RepState> st(e->nrep);
+  std::vector<double> stats((size_t)kStats * e->nrep);
+  CK(e, cudaMemcpy(st.data(), e->d_st, sizeof(RepState) * e->nrep, cudaMemcpyDeviceToHost));
+  for (int r = 0; r < e->nrep; r++) {
+    const RepDev &R = e->rep[r];
+    mcx_replica_desc d;
+    CkptState cs;
+    if (fread(&d, sizeof d, 1, fc.f) != 1 || fread(&cs, sizeof cs, 1, fc.f) != 1 ||
+        fread(stats.data() + (size_t)kStats * r, sizeof(double), kStats, fc.f) != (size_t)kStats)
+      return fail(e, MCX_ERR_PARSE, "mcx_load: %s is truncated", path);
+    const mcx_replica_desc &m = e->desc[r];
+    if (d.nx != m.nx || d.ny != m.ny || d.nz != m.nz || d.geometry != m.geometry || d.potential != m.potential ||
+        d.xbound != m.xbound || d.ybound != m.ybound || d.zbound != m.zbound)
+      return fail(e, MCX_ERR_INVALID, "mcx_load: replica %d of the checkpoint is %dx%dx%d (geometry %d, potential %d), "
+                  "the engine's %dx%dx%d (geometry %d, potential %d)", r, d.nx, d.ny, d.nz, d.geometry, d.potential,
+                  m.nx, m.ny, m.nz, m.geometry, m.potential);
+    std::vector<float> ni(3 * (size_t)R.ntot);
+    if (fread(ni.data(), sizeof(float), ni.size(), fc.f) != ni.size())
+      return fail(e, MCX_ERR_PARSE, "mcx_load: %s is truncated", path);
+    if (e->var.mask) {
+      std::vector<int> pt(R.ntot);
+      std::vector<float> ns(3 * (size_t)R.ntot);
+      if (fread(pt.data(), sizeof(int), pt.size(), fc.f) != pt.size() ||
+          fread(ns.data(), sizeof(float), ns.size(), fc.f) != ns.size())
+        return fail(e, MCX_ERR_PARSE, "mcx_load: %s is truncated", path);
+      if (mcx_status s2 = mcx_set_mask(e, r, pt.data(), ns.data())) return s2;
+    }
+    if (mcx_status s2 = mcx_set_state(e, r, ni.data())) return s2;
+    st[r].T = cs.T;
+    st[r].ang_var = cs.ang_var;
+    st[r].sweep = cs.sweep;
+    st[r].meas = cs.meas;
+    st[r].frozen = cs.frozen;
+    st[r].done = 0;
+    for (int l = 0; l < kLanes; l++) st[r].acc[l] = 0;
+    e->desc[r].T = cs.T;
+  }
+  if (hdr[3] & 1u) {
+    int32_t prop = 0;
+    std::vector<float> w(MCX_MLP_PARAMS);
+    if (fread(&prop, sizeof prop, 1, fc.f) != 1 || fread(w.data(), sizeof(float), w.size(), fc.f) != w.size())
+      return fail(e, MCX_ERR_PARSE, "mcx_load: %s is truncated", path);
+    if (mcx_status s2 = mcx_set_mlp(e, w.data(), MCX_MLP_PARAMS)) return s2;
+    if (mcx_status s2 = mcx_set_proposal(e, prop)) return s2;
+  }
+  CK(e, cudaMemcpyAsync(e->d_st, st.data(), sizeof(RepState) * e->nrep, cudaMemcpyHostToDevice, e->stream));
+  CK(e, cudaMemcpyAsync(e->d_stats, stats.data(), sizeof(double) * stats.size(), cudaMemcpyHostToDevice, e->stream));
+  CK(e, cudaStreamSynchronize(e->stream));
+  e->meas_flushed = st[0].meas;
+  e->pending = 0;
+  return MCX_OK;
+}
+
+// Replica exchange between replicas of the same Hamiltonian at different
+// temperatures: pair (a, b) swaps its temperatures (and step sizes) with
+// probability min(1, exp((1/Ta - 1/Tb)(Ha - Hb))), H the total energy of the
+// current state, u from Philox4x32-10 counter (pair, round_lo, round_hi,
+// TAG_PT), key (seed, 0).
+extern "C" mcx_status mcx_exchange(mcx_engine *e, int n, const int *pairs, unsigned int seed,
+                                   unsigned long long round, int *accepted) {
+  if (!e) return fail(nullptr, MCX_ERR_INVALID, "null engine");
+  if (n < 0 || (n > 0 && !pairs)) return fail(e, MCX_ERR_INVALID, "mcx_exchange: bad pair list");
+  auto same = [](const mcx_replica_desc &x, const mcx_replica_desc &y) {
+    mcx_replica_desc a = x, b = y;
+    a.T = b.T = 0.f;
+    a.ang_var = b.ang_var = 0.f;
+    a.seed = b.seed = 0;
+    a.stream = b.stream = 0;
+    return memcmp(&a, &b, sizeof a) == 0;
+  };
+  std::vector<char> used(e->nrep, 0);
+  for (int i = 0; i < n; i++) {
+    const int a = pairs[2 * i], b = pairs[2 * i + 1];
+    if (a < 0 || b < 0 || a >= e->nrep || b >= e->nrep || a == b || used[a] || used[b])
+      return fail(e, MCX_ERR_INVALID, "mcx_exchange: pair %d (%d, %d) is not two distinct unused replicas", i, a, b);
+    used[a] = used[b] = 1;
+    if (!same(e->desc[a], e->desc[b]))
+      return fail(e, MCX_ERR_INVALID, "mcx_exchange: replicas %d and %d differ in more than T (not one Hamiltonian)", a, b);
+  }
+  std::vector<RepState> st(e->nrep);
+  CK(e, cudaStreamSynchronize(e->stream));
+  CK(e, cudaMemcpy(st.data(), e->d_st, sizeof(RepState) * e->nrep, cudaMemcpyDeviceToHost));
+  for (int i = 0; i < n; i++) {
+    const int a = pairs[2 * i], b = pairs[2 * i + 1];
+    double ma[MCX_MEASURE_LEN], mb[MCX_MEASURE_LEN];
+    if (mcx_status s2 = mcx_measure(e, a, ma)) return s2;
+    if (mcx_status s2 = mcx_measure(e, b, mb)) return s2;
+    const double N = (double)e->rep[a].ntot;
+    const double Ha = ma[MCX_M_E] * N, Hb = mb[MCX_M_E] * N;
+    const double Ta = st[a].T, Tb = st[b].T;
+    const uint4 w = philox4x32_10(make_uint4((uint32_t)i, (uint32_t)round, (uint32_t)(round >> 32), TAG_PT), seed, 0u);
+    const double u = (double)u01(w.x);
+    const double lr = (1.0 / Ta - 1.0 / Tb) * (Ha - Hb);
+    const bool acc = lr >= 0.0 || u < exp(lr);
+    if (accepted) accepted[i] = acc ? 1 : 0;
+    if (acc) {
+      std::swap(st[a].T, st[b].T);
+      std::swap(st[a].ang_var, st[b].ang_var);
+      std::swap(e->desc[a].T, e->desc[b].T);
+    }
+  }
+  for (int q = 0; q < e->nrep; q++) {
+    CK(e, cudaMemcpyAsync((char *)(e->d_st + q) + offsetof(RepState, T), &st[q].T, sizeof(float),
+                          cudaMemcpyHostToDevice, e->stream));
+    CK(e, cudaMemcpyAsync((char *)(e->d_st + q) + offsetof(RepState, ang_var), &st[q].ang_var, sizeof(float),
+                          cudaMemcpyHostToDevice, e->stream));
+  }
+  CK(e, cudaStreamSynchronize(e->stream));
+  return MCX_OK;
+}
+
 extern "C" mcx_status mcx_measure(mcx_engine *e, int r, double *out) {
   if (mcx_status st = check_rep(e, r)) return st;
   if (!out) return fail(e, MCX_ERR_INVALID, "null output");

@@ -593,6 +593,74 @@ __global__ void k_split_to_mask(RepDev R, const uint8_t *__restrict__ pt, const 
   ns_aos[3 * s + 2] = d ? d[2 * R.plane] : 0.f;
 }
 
+// Local order parameter of every site (lattice_order_parameter,
+// src/parameter_order.cpp:62-113): Q over the site and its existing active
+// neighbours, accumulated in FP32 in the reference's order (x-, y-, z-, the
+// site, z+, y+, x+; upper triangle, 3 n_l n_m per point and -1 on the
+// diagonal, over 2 points), its largest eigenvalue by Jacobi in FP64.  NaN at
+// inactive sites (src/io.cpp:66-71).  Natural site order.
+__device__ __forceinline__ bool bound_ok(int &x, int n, int b) {
+  if (x >= 0 && x < n) return true;
+  if (b != BOUND_PERIODIC) return false;
+  x = x < 0 ? x + n : x - n;
+  return true;
+}
+
+__device__ __forceinline__ void site_dir(const RepDev &R, const float *dir, int i, int j, int k, float v[3]) {
+  const int c = (i + j + k) & 1;
+  const long long off = (long long)(j + R.ny * k) * R.hs + (i >> 1);
+  const float *d = dir + R.dir_off + (long long)(c * 3) * R.plane + off;
+  v[0] = d[0];
+  v[1] = d[R.plane];
+  v[2] = d[2 * R.plane];
+}
+
+__device__ __forceinline__ int site_type(const RepDev &R, const uint8_t *pt, int i, int j, int k) {
+  if (pt == nullptr) return 1;
+  const int c = (i + j + k) & 1;
+  return pt[R.pt_off + (long long)c * R.pplane + (long long)(j + R.ny * k) * R.hps + (i >> 1)];
+}
+
+__global__ void k_local_order(RepDev R, const float *__restrict__ dir, const uint8_t *__restrict__ pt,
+                              float *__restrict__ out) {
+  const long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= R.ntot) return;
+  const int i = (int)(s % R.nx), j = (int)((s / R.nx) % R.ny), k = (int)(s / ((long long)R.nx * R.ny));
+  if (site_type(R, pt, i, j, k) == 0) {
+    out[s] = __int_as_float(0x7fc00000);
+    return;
+  }
+  const int d[7][3] = {{-1, 0, 0}, {0, -1, 0}, {0, 0, -1}, {0, 0, 0}, {0, 0, 1}, {0, 1, 0}, {1, 0, 0}};
+  float Q[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  int points = 0;
+  for (int q = 0; q < 7; q++) {
+    int ii = i + d[q][0], jj = j + d[q][1], kk = k + d[q][2];
+    if (!bound_ok(ii, R.nx, R.xb) || !bound_ok(jj, R.ny, R.yb) || !bound_ok(kk, R.nz, R.zb)) continue;
+    if (site_type(R, pt, ii, jj, kk) == 0) continue;
+    float v[3];
+    site_dir(R, dir, ii, jj, kk, v);
+    for (int l = 0; l < 3; l++) {
+      for (int m = 0; m <= l; m++) Q[3 * m + l] += 3.0f * (v[l] * v[m]);
+      Q[4 * l] -= 1.f;
+    }
+    points++;
+  }
+  const float den = 2.0f * (float)points;
+  double Qd[9];
+  Qd[0] = Q[0] / den;
+  Qd[1] = Q[1] / den;
+  Qd[2] = Q[2] / den;
+  Qd[4] = Q[4] / den;
+  Qd[5] = Q[5] / den;
+  Qd[8] = Q[8] / den;
+  Qd[3] = Qd[1];
+  Qd[6] = Qd[2];
+  Qd[7] = Qd[5];
+  double lam, vec[3];
+  jacobi_sym3(Qd, lam, vec);
+  out[s] = (float)lam;
+}
+
 // mode 0: random on the sphere (z = 2u-1 uniform, azimuth 2 pi u') from
 // Philox(site, 0, 0, TAG_IC); mode 1: the fixed director (hx, hy, hz).
 // Inactive sites get (0, 0, 1) (src/ic.cpp:27-86).
@@ -765,6 +833,10 @@ void launch_split_to_mask(const RepDev &R, const uint8_t *pt, const float *ns, i
                           cudaStream_t st) {
   k_split_to_mask<<<blocks_for(R.ntot), 256, 0, st>>>(R, pt, ns, pt_aos, ns_aos);
 }
+void launch_local_order(const RepDev &R, const float *dir, const uint8_t *pt, float *out, cudaStream_t st) {
+  k_local_order<<<(unsigned)((R.ntot + 255) / 256), 256, 0, st>>>(R, dir, pt, out);
+}
+
 void launch_init(const RepDev &R, const uint8_t *pt, float *dir, int mode, uint32_t seed, float fx, float fy, float fz,
                  cudaStream_t st) {
   k_init<<<blocks_for(R.ntot), 256, 0, st>>>(R, pt, dir, mode, seed, fx, fy, fz);

@@ -43,59 +43,13 @@ bool ends_with_ci(const std::string &s, const char *suf, std::string &stem) {
   return false;
 }
 
-// Local order parameter of one site (lattice_order_parameter,
-// src/parameter_order.cpp:62-113): Q over the site and its existing active
-// neighbours, largest eigenvalue by cyclic Jacobi.
-double local_S(const std::vector<float> &ni, const std::vector<int> &pt, int nx, int ny, int nz, int xb, int yb, int zb,
-               int i, int j, int k) {
-  double Q[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-  int points = 0;
-  const int d[7][3] = {{0, 0, 0}, {-1, 0, 0}, {1, 0, 0}, {0, -1, 0}, {0, 1, 0}, {0, 0, -1}, {0, 0, 1}};
-  for (int q = 0; q < 7; q++) {
-    int ii = i + d[q][0], jj = j + d[q][1], kk = k + d[q][2];
-    auto wrap = [](int &x, int n, int b) {
-      if (x < 0 || x >= n) {
-        if (b == MCX_BOUND_PERIODIC) x = (x + n) % n;
-        else return false;
-      }
-      return true;
-    };
-    if (!wrap(ii, nx, xb) || !wrap(jj, ny, yb) || !wrap(kk, nz, zb)) continue;
-    const long s = (long)ii + (long)nx * ((long)jj + (long)ny * kk);
-    if (pt[s] == 0) continue;
-    const double n[3] = {ni[3 * s], ni[3 * s + 1], ni[3 * s + 2]};
-    for (int l = 0; l < 3; l++) {
-      for (int m = 0; m <= l; m++) Q[3 * m + l] += 3.0 * n[l] * n[m];
-      Q[4 * l] -= 1;
-    }
-    points++;
-  }
-  for (int c : {0, 1, 2, 4, 5, 8}) Q[c] /= 2.0 * points;
-  Q[3] = Q[1];
-  Q[6] = Q[2];
-  Q[7] = Q[5];
-  double A[3][3];
-  for (int r = 0; r < 3; r++)
-    for (int c = 0; c < 3; c++) A[r][c] = Q[3 * r + c];
-  for (int it = 0; it < 50; it++) {
-    double off = fabs(A[0][1]) + fabs(A[0][2]) + fabs(A[1][2]);
-    if (off < 1e-15) break;
-    for (int p = 0; p < 2; p++)
-      for (int qq = p + 1; qq < 3; qq++) {
-        if (A[p][qq] == 0) continue;
-        double th = (A[qq][qq] - A[p][p]) / (2 * A[p][qq]);
-        double t = (th >= 0 ? 1 : -1) / (fabs(th) + sqrt(th * th + 1));
-        double c = 1 / sqrt(t * t + 1), s = t * c;
-        for (int r = 0; r < 3; r++) { double x = A[r][p], y = A[r][qq]; A[r][p] = c * x - s * y; A[r][qq] = s * x + c * y; }
-        for (int r = 0; r < 3; r++) { double x = A[p][r], y = A[qq][r]; A[p][r] = c * x - s * y; A[qq][r] = s * x + c * y; }
-      }
-  }
-  return fmax(A[0][0], fmax(A[1][1], A[2][2]));
-}
-
 // print_n (src/io.cpp:50-80): x,y,z,nx,ny,nz,S,pt with S = nan on inactive sites.
+// S: the per-site local order parameter computed on the GPU
+// (mcx_local_order), or null for the initial-condition file, whose S column
+// the reference writes as 1.
 bool write_snapshot(const std::string &path, const std::vector<float> &ni, const std::vector<int> &pt,
-                    const mcx_replica_desc &d, bool with_S) {
+                    const mcx_replica_desc &d, const float *S) {
+  const bool with_S = S != nullptr;
   FILE *f = fopen(path.c_str(), "w");
   if (!f) return false;
   fprintf(f, with_S ? "x,y,z,nx,ny,nz,S,pt\n" : "x,y,z,nx,ny,nz,s,pt\n");
@@ -104,8 +58,7 @@ bool write_snapshot(const std::string &path, const std::vector<float> &ni, const
       for (int i = 0; i < d.nx; i++) {
         const long s = (long)i + (long)d.nx * ((long)j + (long)d.ny * k);
         if (with_S) {
-          const double S = pt[s] ? local_S(ni, pt, d.nx, d.ny, d.nz, d.xbound, d.ybound, d.zbound, i, j, k) : NAN;
-          fprintf(f, "%d,%d,%d,%g,%g,%g,%g,%d\n", i, j, k, ni[3 * s], ni[3 * s + 1], ni[3 * s + 2], (float)S, pt[s]);
+          fprintf(f, "%d,%d,%d,%g,%g,%g,%g,%d\n", i, j, k, ni[3 * s], ni[3 * s + 1], ni[3 * s + 2], S[s], pt[s]);
         } else {
           fprintf(f, "%d,%d,%d,%g,%g,%g,1,%d\n", i, j, k, ni[3 * s], ni[3 * s + 1], ni[3 * s + 2], pt[s]);
         }
@@ -306,7 +259,7 @@ mcx_status run(const char *path, const char *out_dir) {
     }
   };
   const long nsites = (long)d.nx * d.ny * d.nz;
-  std::vector<float> ni(3 * nsites);
+  std::vector<float> ni(3 * nsites), S(nsites);
   std::vector<int> pt(nsites);
   std::vector<float> ns(3 * nsites);
   try {
@@ -351,7 +304,7 @@ mcx_status run(const char *path, const char *out_dir) {
     }
     check(mcx_get_mask(e, 0, pt.data(), ns.data()));
     check(mcx_get_state(e, 0, ni.data()));
-    write_snapshot(dir + "ic.csv", ni, pt, descs[0], false);
+    write_snapshot(dir + "ic.csv", ni, pt, descs[0], nullptr);
     std::vector<FILE *> po(R, nullptr);
     for (int r = 0; r < R; r++) {
       std::string name = r == 0 ? dir + "po.dat" : dir + "po_r" + std::to_string(r) + ".dat";
@@ -391,7 +344,8 @@ mcx_status run(const char *path, const char *out_dir) {
       }
       if (!snap.empty()) {
         check(mcx_get_state(e, 0, ni.data()));
-        write_snapshot(snap, ni, pt, descs[0], true);
+        check(mcx_local_order(e, 0, S.data()));
+        write_snapshot(snap, ni, pt, descs[0], S.data());
       }
     };
     const bool snapshots = getenv("MCX_NO_SNAPSHOTS") == nullptr;

@@ -149,6 +149,10 @@ def lib() -> C.CDLL:
         L.mcx_stream.restype = V
         L.mcx_pass_timing.argtypes = [V, I, C.POINTER(F), C.POINTER(F)]
         L.mcx_sweep_timing.argtypes = [V, I, C.POINTER(F)]
+        L.mcx_local_order.argtypes = [V, I, V]
+        L.mcx_save.argtypes = [V, C.c_char_p]
+        L.mcx_load.argtypes = [V, C.c_char_p]
+        L.mcx_exchange.argtypes = [V, I, V, C.c_uint, C.c_ulonglong, V]
         L.mcx_set_mlp.argtypes = [V, V, I]
         L.mcx_get_mlp.argtypes = [V, V]
         L.mcx_set_proposal.argtypes = [V, I]
@@ -339,6 +343,26 @@ class Engine:
         loss = np.zeros(1, np.float32)
         self._ck(self._L.mcx_mlp_grad(self._h, _p(s), int(s.shape[0]), _p(g), _p(loss)))
         return float(loss[0]), g
+
+    def local_order(self, r: int) -> np.ndarray:
+        """Per-site local order parameter (NaN at inactive sites)."""
+        out = np.zeros(self.sites(r), np.float32)
+        self._ck(self._L.mcx_local_order(self._h, r, _p(out)))
+        return out
+
+    def save(self, path: str):
+        self._ck(self._L.mcx_save(self._h, path.encode()))
+
+    def load(self, path: str):
+        self._ck(self._L.mcx_load(self._h, path.encode()))
+
+    def exchange(self, pairs, seed: int = 0, round: int = 0) -> np.ndarray:
+        """Replica-exchange attempts for the given (a, b) pairs; returns the
+        acceptance decisions."""
+        pr = np.ascontiguousarray(pairs, np.int32).reshape(-1, 2)
+        acc = np.zeros(len(pr), np.int32)
+        self._ck(self._L.mcx_exchange(self._h, len(pr), _p(pr), int(seed) & 0xFFFFFFFF, int(round), _p(acc)))
+        return acc
 
     @property
     def pass_kind(self) -> str:

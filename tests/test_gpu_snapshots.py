@@ -1,0 +1,169 @@
+"""Snapshots, checkpoints, replica exchange and the parameter-file driver.
+
+- mcx_local_order against an FP64 NumPy restatement of
+  lattice_order_parameter (src/parameter_order.cpp:62-113): Q over the site and
+  its existing active neighbours, largest eigenvalue; NaN at inactive sites.
+- mcx_save / mcx_load: a loaded engine continues the saved trajectory bit for
+  bit (same states, step sizes and running sums after more sweeps).
+- mcx_exchange: the decisions are min(1, exp((1/Ta - 1/Tb)(Ha - Hb))) against
+  the documented Philox uniform; accepted pairs swap T.
+- mcx_run_file: ./mc_sim on a small parameter file writes po.dat and the
+  director_field_*.csv snapshots in the reference's formats."""
+import os
+
+import numpy as np
+import pytest
+
+import mcx
+from oracle import oracle as O
+from helpers import desc_from_model, random_state
+
+pytestmark = pytest.mark.gpu
+
+
+def local_S_ref(ni, pt, m):
+    nx, ny, nz = m.nx, m.ny, m.nz
+    xb, yb, zb = m.effective_bounds()
+    N = [nx, ny, nz]
+    B = [xb, yb, zb]
+    out = np.full(m.n, np.nan)
+    for s in np.nonzero(pt)[0]:
+        i, j, k = s % nx, (s // nx) % ny, s // (nx * ny)
+        Q = np.zeros((3, 3))
+        pts = 0
+        for d in ((0, 0, 0), (-1, 0, 0), (1, 0, 0), (0, -1, 0), (0, 1, 0), (0, 0, -1), (0, 0, 1)):
+            c = [i + d[0], j + d[1], k + d[2]]
+            ok = True
+            for ax in range(3):
+                if c[ax] < 0 or c[ax] >= N[ax]:
+                    if B[ax] == "periodic":
+                        c[ax] %= N[ax]
+                    else:
+                        ok = False
+            if not ok:
+                continue
+            t = c[0] + nx * (c[1] + ny * c[2])
+            if pt[t] == 0:
+                continue
+            n = ni[t].astype(np.float64)
+            Q += 3 * np.outer(n, n) - np.eye(3)
+            pts += 1
+        out[s] = np.linalg.eigvalsh(Q / (2 * pts))[-1]
+    return out
+
+
+@pytest.mark.parametrize("m", [O.Model(nx=12, ny=10, nz=8, potential="ll"),
+                               O.Model(nx=16, ny=16, nz=16, geometry="sphere", potential="ll",
+                                       surfaces=[O.Surface("fg", 1.0)]),
+                               O.Model(nx=12, ny=8, nz=6, geometry="slab", potential="ghrl",
+                                       surfaces=[O.Surface("homeotropic", 2.0), O.Surface("fg", 1.0)])],
+                         ids=["bulk", "sphere", "slab"])
+def test_local_order_parameter(m):
+    lat = O.Lattice(m)
+    with mcx.Engine([desc_from_model(m)]) as eng:
+        ni = random_state(m, lat.pt, np.random.default_rng(4))
+        ni = 0.3 * ni + np.array([0.1, 0.2, 0.9], np.float32)
+        ni /= np.linalg.norm(ni, axis=1, keepdims=True)
+        eng.set_state(0, ni)
+        got = eng.local_order(0)
+        ni = eng.get_state(0)
+    want = local_S_ref(ni, lat.pt, m)
+    assert np.array_equal(np.isnan(got), np.isnan(want))
+    ok = ~np.isnan(want)
+    assert np.max(np.abs(got[ok] - want[ok])) < 2e-6
+
+
+def test_checkpoint_continues_the_trajectory(tmp_path):
+    m = O.Model(nx=12, ny=8, nz=6, geometry="slab", potential="ghrl", k11=1.0, k22=0.6, k33=1.4, p0=20, elecA=0.5,
+                elecZ=1.0, elecE=1.0, surfaces=[O.Surface("homeotropic", 2.0), O.Surface("fg", 1.0)])
+    descs = [desc_from_model(m, T=0.9 + 0.1 * r, seed=11 + r, stream=r) for r in range(3)]
+    path = str(tmp_path / "ck.bin")
+    with mcx.Engine(descs) as a:
+        for r in range(3):
+            a.init_random(r, 5 + r)
+        a.sweep(7, measure=True)
+        a.save(path)
+        a.sweep(9, measure=True)
+        want = [(a.get_state(r), a.stats(r)) for r in range(3)]
+    with mcx.Engine(descs) as b:
+        b.load(path)
+        b.sweep(9, measure=True)
+        got = [(b.get_state(r), b.stats(r)) for r in range(3)]
+    for (sa, ta), (sb, tb) in zip(want, got):
+        assert np.array_equal(sa, sb)
+        assert ta[mcx.ST_ANG_VAR] == tb[mcx.ST_ANG_VAR]
+        assert ta[mcx.ST_SWEEP_INDEX] == tb[mcx.ST_SWEEP_INDEX] == 16
+        assert ta[mcx.ST_N] == tb[mcx.ST_N] == 16
+        assert ta[mcx.ST_S1] == pytest.approx(tb[mcx.ST_S1], rel=1e-12)
+        assert ta[mcx.ST_E1] == pytest.approx(tb[mcx.ST_E1], rel=1e-12)
+    with mcx.Engine(descs[:2]) as c:
+        with pytest.raises(mcx.McxError):
+            c.load(path)
+
+
+def test_replica_exchange_decisions():
+    m = O.Model(nx=8, ny=8, nz=8, potential="ll")
+    Ts = [0.6, 0.9, 1.2, 1.5]
+    descs = [desc_from_model(m, T=T, seed=3 + r, stream=r) for r, T in enumerate(Ts)]
+    with mcx.Engine(descs) as eng:
+        for r in range(4):
+            eng.init_random(r, 20 + r)
+        eng.sweep(30)
+        seed, rnd = 77, 5
+        pairs = [(0, 1), (2, 3)]
+        H = [eng.measure(r)["E"] * m.n for r in range(4)]
+        acc = eng.exchange(pairs, seed=seed, round=rnd)
+        for i, (a, b) in enumerate(pairs):
+            u = float(O.u24(O.philox([i, rnd, 0, 4], [seed, 0]))[0])
+            lr = (1 / Ts[a] - 1 / Ts[b]) * (H[a] - H[b])
+            assert bool(acc[i]) == (lr >= 0 or u < np.exp(lr))
+            if acc[i]:
+                assert eng.desc(a)[0].T == np.float32(Ts[b]) and eng.desc(b)[0].T == np.float32(Ts[a])
+            else:
+                assert eng.desc(a)[0].T == np.float32(Ts[a])
+        # equal temperatures always swap
+        eng.set_temperature(1.0)
+        assert np.all(eng.exchange([(0, 1), (2, 3)], seed=1, round=9) == 1)
+        with pytest.raises(mcx.McxError):
+            eng.exchange([(0, 0)])
+    other = [desc_from_model(m, T=1.0), desc_from_model(O.Model(nx=8, ny=8, nz=8, potential="ll", A=2.0), T=1.0)]
+    with mcx.Engine(other) as eng:
+        with pytest.raises(mcx.McxError):
+            eng.exchange([(0, 1)])
+
+
+PARAMS = """Nx  8
+Ny  8
+Nz  8
+potential  ll
+evol  thermalGPU
+Ti    1.2
+Tf    1.0
+dT    -0.1
+MCT  20
+MCS  20
+ic  random
+geometry  bulk
+xbound    periodic
+ybound    periodic
+zbound    periodic
+"""
+
+
+def test_run_file_writes_reference_outputs(tmp_path):
+    pf = tmp_path / "params.txt"
+    pf.write_text(PARAMS)
+    mcx.run_file(str(pf), str(tmp_path) + "/")
+    rows = [ln.split() for ln in (tmp_path / "po.dat").read_text().splitlines()]
+    assert rows[0] == ["T", "S", "varS", "E", "varE"]
+    data = np.array(rows[1:], float)
+    assert data.shape == (3, 5)
+    assert np.allclose(data[:, 0], [1.2, 1.1, 1.0], atol=1e-5)
+    assert np.all((data[:, 1] > 0) & (data[:, 1] <= 1)) and np.all(data[:, 3] < 0)
+    snaps = sorted(f for f in os.listdir(tmp_path) if f.startswith("director_field_"))
+    assert len(snaps) >= 3
+    lines = (tmp_path / snaps[0]).read_text().splitlines()
+    assert lines[0] == "x,y,z,nx,ny,nz,S,pt"
+    assert len(lines) == 1 + 8 ** 3
+    S = np.array([float(l.split(",")[6]) for l in lines[1:]])
+    assert np.all((S >= -0.5) & (S <= 1.0))
