@@ -68,7 +68,7 @@ typedef enum {
   MCX_ERR_PARSE = 6        /* parameter or geometry file is malformed */
 } mcx_status;
 
-typedef enum { MCX_POT_LL = 0, MCX_POT_GHRL = 1 } mcx_potential;
+typedef enum { MCX_POT_LL = 0, MCX_POT_GHRL = 1, MCX_POT_PEAR = 2 } mcx_potential;
 typedef enum { MCX_GEO_BULK = 0, MCX_GEO_SLAB = 1, MCX_GEO_SPHERE = 2, MCX_GEO_CUSTOM = 3 } mcx_geometry;
 typedef enum { MCX_BOUND_FREE = 0, MCX_BOUND_PERIODIC = 1 } mcx_bound;
 typedef enum {
@@ -104,6 +104,7 @@ typedef struct {
   float theta_s[MCX_MAX_SURFACES]; /* degrees */
   float phi_s[MCX_MAX_SURFACES];   /* degrees */
   float radius;                /* sphere: droplet radius; 0 = Nz/2 as the reference */
+  float B1, C;                 /* Pear (splay-bend) potential: polar and splay couplings */
 } mcx_replica_desc;
 
 typedef struct mcx_engine mcx_engine;
@@ -360,6 +361,11 @@ mcx_status mcx_check_file(const char *param_file, mcx_replica_desc *desc);
 #define MCX_NOALLOC_MAX_SITES (1 << 27)
 mcx_status mcx_measure_noalloc(const mcx_replica_desc *desc, const float *d_ni_aos, const int *d_pt,
                                const float *d_ns_aos, double *d_out, void *stream);
+
+/* Polarization of a replica's current state, |sum of directors| / sites over
+ * all sites (Polarization, src/parameter_order.cpp:142-155; the sixth po.dat
+ * column of Pear runs). */
+mcx_status mcx_polarization(mcx_engine *eng, int replica, double *P);
 
 /* Local order parameter of every site of a replica (lattice_order_parameter,
  * src/parameter_order.cpp:62-113, as the snapshot writer print_n,

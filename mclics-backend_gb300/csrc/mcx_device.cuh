@@ -19,7 +19,7 @@ constexpr int kBlock = 256;  // threads per CTA of the pass kernels: one site ea
 constexpr int kLanes = 8;    // atomic lanes per replica (spreads same-address atomics)
 constexpr int kQ = 7;        // measured sums: E_all, E_valid, n_a n_b for xx xy xz yy yz
 
-enum : int { POT_LL = 0, POT_GHRL = 1 };
+enum : int { POT_LL = 0, POT_GHRL = 1, POT_PEAR = 2 };
 enum : int { BOUND_FREE = 0, BOUND_PERIODIC = 1 };
 enum : int {
   ANCH_HOMEOTROPIC = 0,
@@ -61,6 +61,7 @@ struct RepDev {
   long long ns_off;   // float offset of its [2][3][plane] normals
   float A, elecA, elecE, ex, ey, ez;
   float lam, mu, nu, rho, sigma;
+  float B1, C;  // Pear potential
   uint32_t seed, stream;
   int anch[kMaxSurf];
   float W[kMaxSurf];

@@ -213,7 +213,7 @@ static mcx_status check_desc(const mcx_replica_desc &d, int r) {
   if ((long long)d.nx * d.ny * d.nz >= (1LL << 31)) return fail(nullptr, MCX_ERR_INVALID, "replica %d: more than 2^31 sites", r);
   if (d.nx % 2) return fail(nullptr, MCX_ERR_UNSUPPORTED, "replica %d: nx = %d must be even (red/black rows)", r, d.nx);
   if (d.geometry < 0 || d.geometry > 3) return fail(nullptr, MCX_ERR_INVALID, "replica %d: bad geometry %d", r, d.geometry);
-  if (d.potential < 0 || d.potential > 1) return fail(nullptr, MCX_ERR_INVALID, "replica %d: bad potential %d", r, d.potential);
+  if (d.potential < 0 || d.potential > 2) return fail(nullptr, MCX_ERR_INVALID, "replica %d: bad potential %d", r, d.potential);
   if (d.n_surfaces < 0 || d.n_surfaces > MCX_MAX_SURFACES) return fail(nullptr, MCX_ERR_INVALID, "replica %d: bad surface count %d", r, d.n_surfaces);
   for (int s = 0; s < d.n_surfaces; s++)
     if (d.anchoring[s] < 0 || d.anchoring[s] > 7) return fail(nullptr, MCX_ERR_INVALID, "replica %d: bad anchoring %d on surface %d", r, d.anchoring[s], s);
@@ -334,6 +334,8 @@ extern "C" mcx_status mcx_create(int n, const mcx_replica_desc *descs, mcx_engin
     R.ez = d.elecZ;
     float g[5] = {0, 0, 1, 0, 0};
     if (d.potential == MCX_POT_GHRL) ghrl_constants(d.k11, d.k22, d.k33, d.p0, g);
+    R.B1 = d.B1;
+    R.C = d.C;
     R.lam = g[0];
     R.mu = g[1];
     R.nu = g[2];
@@ -957,6 +959,9 @@ static mcx_status upload_mlp(mcx_engine *e, const float *w);
 
 extern "C" mcx_status mcx_set_mlp(mcx_engine *e, const float *w, int n) {
   if (!e) return fail(nullptr, MCX_ERR_INVALID, "null engine");
+  if (e->var.pot == POT_PEAR)
+    return fail(e, MCX_ERR_UNSUPPORTED,
+                "the learned proposal's head-tail symmetric mixture is built for LL and GHRL; the Pear potential is polar");
   if (!w || n != MCX_MLP_PARAMS) return fail(e, MCX_ERR_INVALID, "mcx_set_mlp: expected %d weights, got %d", MCX_MLP_PARAMS, n);
   for (int i = 0; i < n; i++)
     if (!(w[i] == w[i]) || w[i] > 1e30f || w[i] < -1e30f) return fail(e, MCX_ERR_INVALID, "mcx_set_mlp: weight %d is not finite", i);
@@ -1151,6 +1156,20 @@ extern "C" mcx_status mcx_train_mlp(mcx_engine *e, const mcx_train_config *cfg, 
 // ---------------------------------------------------------------------------
 // Snapshots, checkpoints, replica exchange.
 // ---------------------------------------------------------------------------
+extern "C" mcx_status mcx_polarization(mcx_engine *e, int r, double *P) {
+  if (mcx_status st = check_rep(e, r)) return st;
+  if (!P) return fail(e, MCX_ERR_INVALID, "mcx_polarization: null output");
+  launch_polarization(e->rep[r], e->d_dir, e->d_mout, e->stream);
+  e->launches++;
+  CKL(e);
+  double sum[3];
+  CK(e, cudaMemcpyAsync(sum, e->d_mout, sizeof sum, cudaMemcpyDeviceToHost, e->stream));
+  CK(e, cudaStreamSynchronize(e->stream));
+  const double N = (double)e->rep[r].ntot;
+  *P = sqrt(sum[0] * sum[0] + sum[1] * sum[1] + sum[2] * sum[2]) / N;
+  return MCX_OK;
+}
+
 extern "C" mcx_status mcx_local_order(mcx_engine *e, int r, float *S) {
   if (mcx_status st = check_rep(e, r)) return st;
   if (!S) return fail(e, MCX_ERR_INVALID, "mcx_local_order: null output");

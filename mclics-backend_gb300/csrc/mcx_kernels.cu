@@ -736,6 +736,9 @@ int pass_blocks_per_sm(const Variant &v, int mode) {
   if (v.pot == POT_LL) {
     if (v.mask) fn = v.field ? pass_fn<POT_LL, true, true>(mode) : pass_fn<POT_LL, true, false>(mode);
     else fn = v.field ? pass_fn<POT_LL, false, true>(mode) : pass_fn<POT_LL, false, false>(mode);
+  } else if (v.pot == POT_PEAR) {
+    if (v.mask) fn = v.field ? pass_fn<POT_PEAR, true, true>(mode) : pass_fn<POT_PEAR, true, false>(mode);
+    else fn = v.field ? pass_fn<POT_PEAR, false, true>(mode) : pass_fn<POT_PEAR, false, false>(mode);
   } else {
     if (v.mask) fn = v.field ? pass_fn<POT_GHRL, true, true>(mode) : pass_fn<POT_GHRL, true, false>(mode);
     else fn = v.field ? pass_fn<POT_GHRL, false, true>(mode) : pass_fn<POT_GHRL, false, false>(mode);
@@ -747,6 +750,7 @@ int pass_blocks_per_sm(const Variant &v, int mode) {
 
 void launch_pass(const Variant &v, int mode, const PassArgs &a, int nblocks, cudaStream_t st) {
   if (v.pot == POT_LL) launch_pass_p<POT_LL>(v, mode, a, nblocks, st);
+  else if (v.pot == POT_PEAR) launch_pass_p<POT_PEAR>(v, mode, a, nblocks, st);
   else launch_pass_p<POT_GHRL>(v, mode, a, nblocks, st);
 }
 
@@ -780,6 +784,7 @@ static const void *tpass_select(const Variant &v, int mode) {
 int tpass_smem_bytes(int stage_bytes) { return kStages * stage_bytes; }
 
 int tpass_blocks_per_sm(const Variant &v, int mode, int stage_bytes) {
+  if (v.pot == POT_PEAR) return 0;  // the staged pass is built for LL and GHRL only
   const void *fn = tpass_select(v, mode);
   const int smem = tpass_smem_bytes(stage_bytes);
   if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess) return 0;
@@ -789,6 +794,7 @@ int tpass_blocks_per_sm(const Variant &v, int mode, int stage_bytes) {
 }
 
 void launch_tpass(const Variant &v, int mode, const PassArgs &a, int grid, cudaStream_t st) {
+  if (v.pot == POT_PEAR) return;  // never selected for Pear (tpass_blocks_per_sm is 0)
   const int smem = tpass_smem_bytes(a.stage_bytes);
   if (v.pot == POT_LL) {
     if (v.mask) {
@@ -833,6 +839,40 @@ void launch_split_to_mask(const RepDev &R, const uint8_t *pt, const float *ns, i
                           cudaStream_t st) {
   k_split_to_mask<<<blocks_for(R.ntot), 256, 0, st>>>(R, pt, ns, pt_aos, ns_aos);
 }
+// Sum of the directors of every site (the polarization's numerator), FP64.
+__global__ void k_polarization(RepDev R, const float *__restrict__ dir, double *out) {
+  __shared__ double red[3][8];
+  double v[3] = {0, 0, 0};
+  for (long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x; s < 2LL * R.plane; s += (long long)gridDim.x * blockDim.x) {
+    const int c = (int)(s / R.plane);
+    const long long o = s - (long long)c * R.plane;
+    const long long row = o / R.hs;
+    const int h = (int)(o - row * R.hs);
+    const int j = (int)(row % R.ny), k = (int)(row / R.ny);
+    const int i = 2 * h + ((c + j + k) & 1);
+    if (h >= R.hx || i >= R.nx) continue;  // row padding
+    const float *d = dir + R.dir_off + (long long)(c * 3) * R.plane + o;
+    v[0] += d[0];
+    v[1] += d[R.plane];
+    v[2] += d[2 * R.plane];
+  }
+  for (int q = 0; q < 3; q++) {
+    for (int off = 16; off > 0; off >>= 1) v[q] += __shfl_xor_sync(0xffffffffu, v[q], off);
+    if ((threadIdx.x & 31) == 0) red[q][threadIdx.x >> 5] = v[q];
+  }
+  __syncthreads();
+  if (threadIdx.x < 3) {
+    double t = 0;
+    for (int w = 0; w < 8; w++) t += red[threadIdx.x][w];
+    atomicAdd(out + threadIdx.x, t);
+  }
+}
+
+void launch_polarization(const RepDev &R, const float *dir, double *out, cudaStream_t st) {
+  cudaMemsetAsync(out, 0, 3 * sizeof(double), st);
+  k_polarization<<<256, 256, 0, st>>>(R, dir, out);
+}
+
 void launch_local_order(const RepDev &R, const float *dir, const uint8_t *pt, float *out, cudaStream_t st) {
   k_local_order<<<(unsigned)((R.ntot + 255) / 256), 256, 0, st>>>(R, dir, pt, out);
 }

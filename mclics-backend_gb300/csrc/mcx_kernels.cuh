@@ -106,6 +106,8 @@ void launch_split_to_mask(const RepDev &R, const uint8_t *pt, const float *ns, i
                           cudaStream_t st);
 void launch_init(const RepDev &R, const uint8_t *pt, float *dir, int mode, uint32_t seed, float fx, float fy, float fz,
                  cudaStream_t st);
+// Sum of every site's director (3 doubles at out).
+void launch_polarization(const RepDev &R, const float *dir, double *out, cudaStream_t st);
 // Per-site local order parameter (natural order; NaN at inactive sites).
 void launch_local_order(const RepDev &R, const float *dir, const uint8_t *pt, float *out, cudaStream_t st);
 

@@ -506,6 +506,11 @@ static const void *march_fn_v(const Variant &v, int mode) {
       return v.field ? march_fn<POT_LL, true, true, NT, false>(mode) : march_fn<POT_LL, true, false, NT, false>(mode);
     return v.field ? march_fn_unmasked<POT_LL, true, NT>(v, mode) : march_fn_unmasked<POT_LL, false, NT>(v, mode);
   }
+  if (v.pot == POT_PEAR) {
+    if (v.mask)
+      return v.field ? march_fn<POT_PEAR, true, true, NT, false>(mode) : march_fn<POT_PEAR, true, false, NT, false>(mode);
+    return v.field ? march_fn_unmasked<POT_PEAR, true, NT>(v, mode) : march_fn_unmasked<POT_PEAR, false, NT>(v, mode);
+  }
   if (v.mask)
     return v.field ? march_fn<POT_GHRL, true, true, NT, false>(mode) : march_fn<POT_GHRL, true, false, NT, false>(mode);
   return v.field ? march_fn_unmasked<POT_GHRL, true, NT>(v, mode) : march_fn_unmasked<POT_GHRL, false, NT>(v, mode);
@@ -547,7 +552,7 @@ static const void *tmarch_kernel(const Variant &v, int mode, int nt) {
 int tmarch_smem_bytes(const PassArgs &a) { return (4 * a.tm_o + 2 * a.tm_a) * 4; }
 
 bool tmarch_prepare(const Variant &v, int nt, int smem_bytes) {
-  if (v.mask) return false;
+  if (v.mask || v.pot == POT_PEAR) return false;  // built for unmasked LL and GHRL
   for (int mode : {MODE_SWEEP, MODE_SWEEP_MEASURE})
     if (cudaFuncSetAttribute(tmarch_kernel(v, mode, nt), cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes) !=
         cudaSuccess)
@@ -560,6 +565,7 @@ bool tmarch_prepare(const Variant &v, int nt, int smem_bytes) {
 }
 
 void launch_tmarch(const Variant &v, int mode, const PassArgs &a, int nt, bool pdl, cudaStream_t st) {
+  if (v.mask || v.pot == POT_PEAR) return;  // never selected there (tmarch_prepare is false)
   PassArgs args = a;
   void *params[] = {&args};
   cudaLaunchConfig_t cfg = {};

@@ -36,6 +36,14 @@ __device__ __forceinline__ float bond(const RepDev &R, float ax, float ay, float
   if (POT == POT_LL) {
     const float nij = ax * b[0] + ay * b[1] + az * b[2];
     return -1.5f * R.A * nij * nij;
+  } else if (POT == POT_PEAR) {
+    // src/potential.cpp:10-15: -A nij^2 - B1 nij - (C/4)(1 + 2 nij + nij^2)((nj - ni) . rij),
+    // rij = +-(unit vector of the slot's axis)
+    const float nij = ax * b[0] + ay * b[1] + az * b[2];
+    constexpr int X = D >> 1;
+    const float d = (X == 0 ? b[0] - ax : (X == 1 ? b[1] - ay : b[2] - az)) * ((D & 1) ? -1.f : 1.f);
+    const float splay = (1.f + 2.f * nij + nij * nij) * d;
+    return -R.A * nij * nij - R.B1 * nij - (R.C * 0.25f) * splay;
   } else {
     return ghrl_bond<(D >> 1)>(R, ax, ay, az, b[0], b[1], b[2], (D & 1) ? -1.f : 1.f);
   }

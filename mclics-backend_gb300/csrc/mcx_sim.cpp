@@ -141,14 +141,15 @@ mcx_status prepare(const char *path, SimParams &P, mcx_replica_desc &d, std::vec
     d.potential = MCX_POT_LL;
   else if (strcasecmp(P.potential.c_str(), "ghrl") == 0 || strcasecmp(P.potential.c_str(), "grun-hess") == 0)
     d.potential = MCX_POT_GHRL;
-  else if (strcasecmp(P.potential.c_str(), "pear") == 0) {
-    g_err = "potential 'pear' is not implemented by the GB300 engine";
-    return MCX_ERR_UNSUPPORTED;
-  } else {
-    g_err = "potential '" + P.potential + "' not implemented. Options: ll | ghrl";
+  else if (strcasecmp(P.potential.c_str(), "pear") == 0)
+    d.potential = MCX_POT_PEAR;
+  else {
+    g_err = "potential '" + P.potential + "' not implemented. Options: ll | ghrl | pear";
     return MCX_ERR_PARSE;
   }
   d.A = P.A;
+  d.B1 = P.B1;
+  d.C = P.C;
   d.k11 = P.k11;
   d.k22 = P.k22;
   d.k33 = P.k33;
@@ -315,7 +316,10 @@ mcx_status run(const char *path, const char *out_dir) {
           if (f) fclose(f);
         return MCX_ERR_IO;
       }
-      fprintf(po[r], im == 0 || im == 3 ? "T S varS E varE\n" : "ii S varS E varE\n");
+      // Pear runs add the polarization of the block's final state
+      // (src/evolve_thermal.cpp:50-53,82-84)
+      const char *cols = descs[0].potential == MCX_POT_PEAR ? " S varS E varE P\n" : " S varS E varE\n";
+      fprintf(po[r], "%s%s", im == 0 || im == 3 ? "T" : "ii", cols);
       fflush(po[r]);
     }
     struct PoGuard {
@@ -337,9 +341,15 @@ mcx_status run(const char *path, const char *out_dir) {
         const double S1 = stt[MCX_ST_S1] / n, S2 = stt[MCX_ST_S2] / n;
         const double E = stt[MCX_ST_E1] / n, E2 = stt[MCX_ST_E2] / n;
         if (label_fmt[1] == 'd')
-          fprintf(po[r], "%d %g %g %g %g\n", ilabel, S1, S2 - S1 * S1, E, E2 - E * E);
+          fprintf(po[r], "%d %g %g %g %g", ilabel, S1, S2 - S1 * S1, E, E2 - E * E);
         else
-          fprintf(po[r], "%g %g %g %g %g\n", label, S1, S2 - S1 * S1, E, E2 - E * E);
+          fprintf(po[r], "%g %g %g %g %g", label, S1, S2 - S1 * S1, E, E2 - E * E);
+        if (descs[0].potential == MCX_POT_PEAR) {
+          double Pz = 0;
+          check(mcx_polarization(e, r, &Pz));
+          fprintf(po[r], " %g", (float)Pz);
+        }
+        fprintf(po[r], "\n");
         fflush(po[r]);
       }
       if (!snap.empty()) {

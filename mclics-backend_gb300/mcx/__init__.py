@@ -24,7 +24,7 @@ LIB_PATH = os.environ.get("MCX_LIB") or os.path.join(PKG, "_build", "libmcx.so")
 CLI_PATH = os.path.join(PKG, "_build", "mc_sim_gb300")
 
 MAX_SURFACES = 16
-POTENTIALS = {"ll": 0, "lebwohl-lahser": 0, "ghrl": 1, "grun-hess": 1}
+POTENTIALS = {"ll": 0, "lebwohl-lahser": 0, "ghrl": 1, "grun-hess": 1, "pear": 2}
 GEOMETRIES = {"bulk": 0, "slab": 1, "sphere": 2, "custom": 3}
 BOUNDS = {"free": 0, "periodic": 1}
 ANCHORINGS = {"homeotropic": 0, "fg": 1, "rp": 2, "strong": 3, "homeotropic_ghrl": 4, "fg_ghrl": 5, "rp_ghrl": 6,
@@ -67,6 +67,7 @@ class ReplicaDesc(C.Structure):
         ("theta_s", C.c_float * MAX_SURFACES),
         ("phi_s", C.c_float * MAX_SURFACES),
         ("radius", C.c_float),
+        ("B1", C.c_float), ("C", C.c_float),
     ]
 
 
@@ -78,7 +79,8 @@ class TrainConfig(C.Structure):
 
 def replica(nx=16, ny=16, nz=16, geometry="bulk", xbound="periodic", ybound="periodic", zbound="periodic",
             potential="ll", A=1.0, k11=1.0, k22=1.0, k33=1.0, p0=0.0, elecA=0.0, elecX=0.0, elecY=0.0, elecZ=0.0,
-            elecE=1.0, T=1.0, ang_var=0.5, seed=1, stream=0, surfaces: Sequence[dict] = (), radius=0.0) -> ReplicaDesc:
+            elecE=1.0, T=1.0, ang_var=0.5, seed=1, stream=0, surfaces: Sequence[dict] = (), radius=0.0,
+            B1=0.04, C=0.3) -> ReplicaDesc:
     """A replica descriptor from the reference's parameter names.  `surfaces`
     is a list of dicts with keys anchoring, W, theta_s, phi_s (surface id =
     list index = pt - 2)."""
@@ -97,6 +99,7 @@ def replica(nx=16, ny=16, nz=16, geometry="bulk", xbound="periodic", ybound="per
         d.theta_s[i] = s.get("theta_s", 0.0)
         d.phi_s[i] = s.get("phi_s", 0.0)
     d.radius = radius
+    d.B1, d.C = B1, C
     return d
 
 
@@ -150,6 +153,7 @@ def lib() -> C.CDLL:
         L.mcx_pass_timing.argtypes = [V, I, C.POINTER(F), C.POINTER(F)]
         L.mcx_sweep_timing.argtypes = [V, I, C.POINTER(F)]
         L.mcx_local_order.argtypes = [V, I, V]
+        L.mcx_polarization.argtypes = [V, I, C.POINTER(C.c_double)]
         L.mcx_save.argtypes = [V, C.c_char_p]
         L.mcx_load.argtypes = [V, C.c_char_p]
         L.mcx_exchange.argtypes = [V, I, V, C.c_uint, C.c_ulonglong, V]
@@ -343,6 +347,11 @@ class Engine:
         loss = np.zeros(1, np.float32)
         self._ck(self._L.mcx_mlp_grad(self._h, _p(s), int(s.shape[0]), _p(g), _p(loss)))
         return float(loss[0]), g
+
+    def polarization(self, r: int) -> float:
+        P = C.c_double()
+        self._ck(self._L.mcx_polarization(self._h, r, C.byref(P)))
+        return P.value
 
     def local_order(self, r: int) -> np.ndarray:
         """Per-site local order parameter (NaN at inactive sites)."""

@@ -132,6 +132,14 @@ double orc_pair(const orc_params *p, const double ni[3], const double nj[3], int
     if (abs_out) *abs_out = fabs(e);
     return e;
   }
+  if (p->potential == ORC_POT_PEAR) {
+    /* src/potential.cpp:10-15: -A nij^2 - B1 nij - (C/4) (1 + 2 nij + nij^2) ((nj - ni) . rij) */
+    double nij = dot3(ni, nj);
+    double ps = (1 + 2 * nij + nij * nij) * ((nj[0] - ni[0]) * r[0] + (nj[1] - ni[1]) * r[1] + (nj[2] - ni[2]) * r[2]);
+    double t1 = -p->A * nij * nij, t2 = -p->B1 * nij, t3 = -(p->C * 0.25) * ps;
+    if (abs_out) *abs_out = fabs(t1) + fabs(t2) + fabs(t3);
+    return t1 + t2 + t3;
+  }
   /* src/potential.cpp:22-38 */
   double ai = dot3(ni, r), aj = dot3(nj, r), nij = dot3(ni, nj);
   return ghrl_form(p, ai, aj, nij, cross_ref(ni, nj, r), 1.0 / 9.0, abs_out);

@@ -11,7 +11,7 @@
 extern "C" {
 #endif
 
-enum { ORC_POT_LL = 0, ORC_POT_GHRL = 1 };
+enum { ORC_POT_LL = 0, ORC_POT_GHRL = 1, ORC_POT_PEAR = 2 };
 enum { ORC_BOUND_FREE = 0, ORC_BOUND_PERIODIC = 1 };
 enum { ORC_GEO_BULK = 0, ORC_GEO_SLAB = 1, ORC_GEO_SPHERE = 2, ORC_GEO_CUSTOM = 3 };
 enum {
@@ -40,6 +40,7 @@ typedef struct {
   int anch[ORC_MAX_SURF];
   double W[ORC_MAX_SURF];
   double dir[ORC_MAX_SURF][3];
+  double B1, C; /* Pear potential */
 } orc_params;
 
 typedef struct {

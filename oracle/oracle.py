@@ -22,7 +22,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libmcx_oracle.so")
 REF_LIB_PATH = os.path.join(HERE, "_ref", "libref_mcx.so")
 
-POT = {"ll": 0, "lebwohl-lahser": 0, "ghrl": 1, "grun-hess": 1}
+POT = {"ll": 0, "lebwohl-lahser": 0, "ghrl": 1, "grun-hess": 1, "pear": 2}
 GEO = {"bulk": 0, "slab": 1, "sphere": 2, "custom": 3}
 BOUND = {"free": 0, "periodic": 1}
 ANCH = {
@@ -53,6 +53,7 @@ class _Params(C.Structure):
         ("anch", C.c_int * MAX_SURF),
         ("W", C.c_double * MAX_SURF),
         ("dir", (C.c_double * 3) * MAX_SURF),
+        ("B1", C.c_double), ("C", C.c_double),
     ]
 
 
@@ -122,6 +123,8 @@ class Model:
     elecE: float = 1.0
     surfaces: List[Surface] = field(default_factory=list)
     radius: float = 0.0
+    B1: float = 0.04  # Pear potential (include/parameters.h:34-36 defaults)
+    C: float = 0.3
 
     @property
     def n(self) -> int:
@@ -151,6 +154,7 @@ class Model:
         p.lam, p.mu, p.nu, p.rho, p.sigma = float(lam), float(mu), float(nu), float(rho), float(sigma)
         f = lambda v: float(np.float32(v))
         p.elecA, p.elecE, p.ex, p.ey, p.ez = f(self.elecA), f(self.elecE), f(self.elecX), f(self.elecY), f(self.elecZ)
+        p.B1, p.C = f(self.B1), f(self.C)
         p.nsurf = len(self.surfaces)
         for i, s in enumerate(self.surfaces):
             p.anch[i] = ANCH[s.anchoring.lower()]

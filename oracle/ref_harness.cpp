@@ -223,6 +223,13 @@ extern "C" float ref_order(const float *ni, float Q[9], float vec[3]) {
 
 extern "C" int ref_max_threads(void) { return (int)RNG.size(); }
 
+/* The Pear potential (src/simulator.cpp:95-97) with its B1 and C, after ref_setup. */
+extern "C" void ref_set_pear(float B1, float C) {
+  P->B1 = B1;
+  P->C = C;
+  G->bulk_potential = &Bulk_Energy_Selinger_Pear;
+}
+
 /* Re-seeds the per-thread generators as thermalEvolveN::run does
  * (src/evolve_thermal.cpp:40-45): seed * 104729 + thread. */
 extern "C" void ref_seed(unsigned long seed) {

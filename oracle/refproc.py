@@ -53,6 +53,9 @@ def _setup(L, m: dict):
                      _p(W), _p(th), _p(ph), m.get("bound_file", b"").encode() if m.get("bound_file") else None)
     if rc != 0:
         raise RuntimeError("ref_setup failed")
+    if m["potential"] == "pear":
+        L.ref_set_pear.argtypes = [C.c_float, C.c_float]
+        L.ref_set_pear(f(m["B1"]), f(m["C"]))
 
 
 def _worker(m: dict, ops: List[tuple]) -> List[Any]:

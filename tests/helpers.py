@@ -11,7 +11,7 @@ def desc_from_model(m: O.Model, T=1.0, seed=1, stream=0, ang_var=0.5):
                        elecA=m.elecA, elecX=m.elecX, elecY=m.elecY, elecZ=m.elecZ, elecE=m.elecE, T=T,
                        ang_var=ang_var, seed=seed, stream=stream,
                        surfaces=[dict(anchoring=s.anchoring, W=s.W, theta_s=s.theta_s, phi_s=s.phi_s)
-                                 for s in m.surfaces], radius=m.radius)
+                                 for s in m.surfaces], radius=m.radius, B1=m.B1, C=m.C)
 
 
 def random_state(m: O.Model, pt: np.ndarray, rng) -> np.ndarray:

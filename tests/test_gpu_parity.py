@@ -47,6 +47,10 @@ CASES = {
                               surfaces=[O.Surface("fg_ghrl", 1.5), O.Surface("rp_ghrl", 2.0, 20, 70)]),
     "custom_mixed": _custom_model(),
     "bulk_ll_x_periodic_yz_free": O.Model(nx=14, ny=5, nz=3, xbound="periodic", ybound="free", zbound="free"),
+    "bulk_pear_field": O.Model(nx=12, ny=8, nz=6, potential="pear", A=1.0, B1=0.3, C=0.3, elecA=0.4, elecZ=1.0,
+                               elecE=1.0),
+    "sphere_pear_homeotropic": O.Model(nx=12, ny=12, nz=12, geometry="sphere", potential="pear", B1=0.3, C=0.3,
+                                       surfaces=[O.Surface("homeotropic", 4.0)]),
 }
 
 
@@ -104,6 +108,8 @@ def _check_pass(m, lat, before, dE_g, acc_g, prop_g, after, T, ang, seed, stream
 @pytest.mark.parametrize("name", list(CASES))
 def test_pass_parity(name, staged):
     T, ang, seed, stream = 0.8, 0.6, 77, 3
+    if staged and CASES[name].potential == "pear":
+        pytest.skip("the staged pass is built for LL and GHRL")
     m, lat, eng, ni0 = _setup(name, T, seed, stream, ang)
     with eng:
         eng.staged = staged
@@ -133,7 +139,8 @@ def test_measure_parity(name):
         assert abs(abs(np.dot(g["director"], o["director"])) - 1) < 1e-5
 
 
-@pytest.mark.parametrize("name", ["bulk_ll", "sphere_ghrl_fg_field", "custom_mixed", "slab_ghrl_padded"])
+@pytest.mark.parametrize("name", ["bulk_ll", "sphere_ghrl_fg_field", "custom_mixed", "slab_ghrl_padded",
+                                  "sphere_pear_homeotropic"])
 def test_sweeps_and_step_rule_match_oracle(name):
     """Three measured sweeps through the graph-free path: same states, same
     step-size sequence, same running sums as the oracle's red/black sweeps."""

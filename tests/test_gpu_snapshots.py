@@ -167,3 +167,25 @@ def test_run_file_writes_reference_outputs(tmp_path):
     assert len(lines) == 1 + 8 ** 3
     S = np.array([float(l.split(",")[6]) for l in lines[1:]])
     assert np.all((S >= -0.5) & (S <= 1.0))
+
+
+def test_polarization():
+    m = O.Model(nx=12, ny=10, nz=8, potential="pear", B1=0.3, C=0.3)
+    with mcx.Engine([desc_from_model(m)]) as eng:
+        ni = random_state(m, np.ones(m.n, np.int32), np.random.default_rng(9))
+        ni = 0.5 * ni + np.array([0.0, 0.3, 0.8], np.float32)
+        ni /= np.linalg.norm(ni, axis=1, keepdims=True)
+        eng.set_state(0, ni)
+        got = eng.polarization(0)
+        ni = eng.get_state(0).astype(np.float64)
+    assert got == pytest.approx(np.linalg.norm(ni.sum(0)) / m.n, rel=1e-9)
+
+
+def test_run_file_pear_adds_polarization(tmp_path):
+    pf = tmp_path / "params.txt"
+    pf.write_text(PARAMS.replace("potential  ll", "potential  pear\nA 1.0\nB1 0.3\nC 0.3"))
+    mcx.run_file(str(pf), str(tmp_path) + "/")
+    rows = [ln.split() for ln in (tmp_path / "po.dat").read_text().splitlines()]
+    assert rows[0] == ["T", "S", "varS", "E", "varE", "P"]
+    data = np.array(rows[1:], float)
+    assert data.shape == (3, 6) and np.all((data[:, 5] >= 0) & (data[:, 5] <= 1))

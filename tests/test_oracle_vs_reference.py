@@ -41,10 +41,10 @@ def test_masks_bit_exact(geo, dims):
     assert np.array_equal(lat.ns, ns)
 
 
-@pytest.mark.parametrize("pot", ["ll", "ghrl"])
+@pytest.mark.parametrize("pot", ["ll", "ghrl", "pear"])
 def test_pair_energies(pot):
     rng = np.random.default_rng(5)
-    m = _ghrl_model(potential=pot, A=1.3)
+    m = _ghrl_model(potential=pot, A=1.3, B1=0.3, C=0.45)
     a = O.random_directors(600, rng)
     b = O.random_directors(600, rng)
     r = np.tile(RIJ, (100, 1))
@@ -87,6 +87,8 @@ CASES = [
     dict(geometry="slab", potential="ghrl", surfaces=[O.Surface("fg_ghrl", 1.5), O.Surface("homeotropic_ghrl", 2.0)]),
     dict(geometry="sphere", potential="ghrl", surfaces=[O.Surface("fg", 2.0)], elecA=0.3, elecZ=1.0, elecE=2.0),
     dict(geometry="sphere", potential="ll", surfaces=[O.Surface("rp", 1.0, theta_s=60, phi_s=10)]),
+    dict(geometry="bulk", potential="pear", B1=0.3, C=0.3),
+    dict(geometry="sphere", potential="pear", B1=0.3, C=0.3, surfaces=[O.Surface("homeotropic", 4.0)]),
 ]
 
 
