@@ -50,6 +50,7 @@ struct RepDev {
   int pplane; // point-type bytes per colour, hps*ny*nz
   int ncta;   // CTAs of this replica in one direct pass launch
   int mcta;   // CTAs of this replica in one z-march pass launch
+  int lcta;   // CTAs of this replica in one learned z-march pass launch
   uint32_t hp_m, ny_m;  // n / hp == (n * hp_m) >> hp_p for n < 2^31
   int hp_p, ny_p;
   // tiles of the staged pass: tj x tk rows (tj | ny, tk | nz), ntile per colour

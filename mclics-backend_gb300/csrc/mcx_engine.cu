@@ -73,6 +73,10 @@ struct mcx_engine {
   int march_nt = 128, march_k = 8;
   bool pdl = true;  // programmatic dependent launch of the z-march passes
   bool tmarch = false;  // the z-march with rows staged by bulk copies (unmasked lattices)
+  // learned-proposal z-march: its own units (128 pairs x kLearnPlanes planes)
+  std::vector<int4> lunits;
+  int4 *d_lunits = nullptr;
+  bool lmarch_ok = false;
   int tm_o = 0, tm_a = 0;  // its shared-memory slot sizes (floats)
   std::vector<int4> units;
   int4 *d_units = nullptr;
@@ -194,6 +198,7 @@ static void free_engine(mcx_engine *e) {
   cudaFree(e->d_err);
   cudaFree(e->d_mlp);
   cudaFree(e->d_units);
+  cudaFree(e->d_lunits);
   cudaFree(e->d_w);
   cudaFree(e->d_am);
   cudaFree(e->d_av);
@@ -676,8 +681,15 @@ static PassArgs pass_args(mcx_engine *e) {
 static void launch_sweep_pass(mcx_engine *e, PassArgs &pa, int colour, bool measure) {
   pa.colour = colour;
   const int mode = measure ? MODE_SWEEP_MEASURE : MODE_SWEEP;
-  if (e->proposal == MCX_PROPOSAL_VMF_MLP) launch_pass_learned(e->var, mode, pa, e->lgrid[mode], e->stream);
-  else if (e->staged) launch_tpass(e->var, mode, pa, e->grid[measure ? 1 : 0], e->stream);
+  if (e->proposal == MCX_PROPOSAL_VMF_MLP) {
+    if (e->march && e->lmarch_ok) {
+      pa.units = e->d_lunits;
+      pa.nunits = (int)e->lunits.size();
+      launch_lmarch(e->var, mode, pa, e->pdl, e->stream);
+    } else {
+      launch_pass_learned(e->var, mode, pa, e->lgrid[mode], e->stream);
+    }
+  } else if (e->staged) launch_tpass(e->var, mode, pa, e->grid[measure ? 1 : 0], e->stream);
   else if (e->march && e->tmarch) launch_tmarch(e->var, mode, pa, e->march_nt, e->pdl, e->stream);
   else if (e->march) launch_march(e->var, mode, pa, e->march_nt, e->pdl, e->stream);
   else launch_pass(e->var, mode, pa, e->pgrid[mode], e->stream);
@@ -797,6 +809,33 @@ extern "C" int mcx_get_staged(const mcx_engine *e) { return e && e->staged ? 1 :
 
 // Re-plans the z-march units for a block size and chunk depth and uploads
 // them with the replicas' CTA counts.
+// Units of the learned-proposal z-march: per replica, blocks of its CTA size
+// of a plane's pairs times chunks of kLearnPlanes planes; uploads them and the
+// replicas' CTA counts.
+constexpr int kLearnPlanes = 8;
+static mcx_status plan_lmarch(mcx_engine *e) {
+  e->lunits.clear();
+  const int nt = lmarch_block_threads();
+  for (int r = 0; r < e->nrep; r++) {
+    RepDev &R = e->rep[r];
+    const int npp = R.hp * R.ny, K = std::min(kLearnPlanes, R.nz);
+    R.lcta = 0;
+    for (int k0 = 0; k0 < R.nz; k0 += K)
+      for (int p0 = 0; p0 < npp; p0 += nt) {
+        e->lunits.push_back(make_int4(r, p0, k0, std::min(K, R.nz - k0)));
+        R.lcta++;
+      }
+  }
+  cudaFree(e->d_lunits);
+  e->d_lunits = nullptr;
+  CK(e, cudaMalloc(&e->d_lunits, sizeof(int4) * e->lunits.size()));
+  CK(e, cudaMemcpyAsync(e->d_lunits, e->lunits.data(), sizeof(int4) * e->lunits.size(), cudaMemcpyHostToDevice,
+                        e->stream));
+  CK(e, cudaMemcpyAsync(e->d_rep, e->rep.data(), sizeof(RepDev) * e->nrep, cudaMemcpyHostToDevice, e->stream));
+  CK(e, cudaStreamSynchronize(e->stream));
+  return MCX_OK;
+}
+
 // Shared-memory slots of the TMA-staged z-march for the current units: an O
 // slot holds 3 components x (rows spanned + 2) rows, an A slot 3 x rows.
 static void plan_tmarch_slots(mcx_engine *e) {
@@ -990,6 +1029,10 @@ static mcx_status upload_mlp(mcx_engine *e, const float *w) {
       if (per <= 0) return fail(e, MCX_ERR_CUDA, "learned pass kernel cannot be resident");
       e->lgrid[m] = (int)std::min<long long>((long long)per * nsm, (long long)e->map.size());
     }
+    const char *lm = getenv("MCX_LMARCH");
+    e->lmarch_ok = !(lm && atoi(lm) == 0) && lmarch_prepare(e->var);
+    if (e->lmarch_ok)
+      if (mcx_status st = plan_lmarch(e)) return st;
   }
   CK(e, cudaMemcpy(e->d_mlp, packed.data(), packed.size(), cudaMemcpyHostToDevice));
   return MCX_OK;

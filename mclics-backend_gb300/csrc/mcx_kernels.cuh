@@ -83,6 +83,11 @@ bool tmarch_prepare(const Variant &v, int nt, int smem_bytes);
 int tmarch_smem_bytes(const PassArgs &a);
 void launch_tmarch(const Variant &v, int mode, const PassArgs &a, int nt, bool pdl, cudaStream_t st);
 int march_blocks_per_sm(const Variant &v, int mode, int nt);
+// The learned-proposal z-march (mcx_lmarch.cu): units of lmarch_block_threads()
+// pairs; lmarch_prepare sets its shared memory and checks residency.
+int lmarch_block_threads();
+bool lmarch_prepare(const Variant &v);
+void launch_lmarch(const Variant &v, int mode, const PassArgs &a, bool pdl, cudaStream_t st);
 // The direct pass with the learned proposal (mcx_learned.cu).
 void launch_pass_learned(const Variant &v, int mode, const PassArgs &a, int nblocks, cudaStream_t st);
 int pass_learned_blocks_per_sm(const Variant &v, int mode);

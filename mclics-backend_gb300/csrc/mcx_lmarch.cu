@@ -1,0 +1,227 @@
+// mcx_lmarch.cu -- the learned-proposal pass as a z-march (no counterpart in
+// the reference).
+//
+//   k_lmarch  the z-march of mcx_march.cu with the learned proposal: per
+//             plane every thread loads its pair's neighbourhood into
+//             registers (the z neighbours come from the march), writes the two
+//             sites' network inputs as rows 2*lane and 2*lane+1 of its warp's
+//             64-row tile, the warp evaluates the network on the tensor cores
+//             (mlp_warp, mcx_mlp.cuh), and each thread draws and accepts its
+//             sites' moves (site_update_learned, mcx_pass.cuh).  The network is
+//             warp-synchronous, so every lane runs every plane: a thread past
+//             the end of the plane contributes zero rows and updates nothing.
+//             No shared-memory staging of neighbourhoods: 40 KB per CTA
+//             (weights and one input/output tile per warp), four CTAs of 128
+//             threads per SM at 128 registers.
+//
+// Results are bit-identical to the learned direct pass (k_pass<LEARN>): the
+// same rows reach the network, the same per-site Philox counters drive the
+// draws.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include "mcx_march.cuh"
+#include "mcx_mlp.cuh"
+
+namespace mcx {
+
+constexpr int kLPB = 128;  // threads per CTA (4 warps)
+constexpr int kLmarchSmem = kMlpBytes + (kLPB / 32) * (64 * kXs * 2 + 64 * 4 * 4);
+#ifndef MCX_LMARCH_MIN_BLOCKS
+#define MCX_LMARCH_MIN_BLOCKS 4
+#endif
+
+template <int POT, bool MASK, bool FIELD, int MODE>
+__global__ void __launch_bounds__(kLPB, MCX_LMARCH_MIN_BLOCKS) k_lmarch(PassArgs a) {
+  static_assert(MODE == MODE_SWEEP || MODE == MODE_SWEEP_MEASURE, "sweep modes only");
+  extern __shared__ __align__(16) uint8_t dyn[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint8_t *W = dyn;
+  __nv_bfloat16 *X = reinterpret_cast<__nv_bfloat16 *>(dyn + kMlpBytes) + (size_t)warp * 64 * kXs;
+  float *Y = reinterpret_cast<float *>(dyn + kMlpBytes + (kLPB / 32) * 64 * kXs * 2) + (size_t)warp * 64 * 4;
+  // the weights are written only between launches (host copies on the stream)
+  for (int i = threadIdx.x; i < kMlpBytes / 16; i += kLPB)
+    reinterpret_cast<int4 *>(W)[i] = reinterpret_cast<const int4 *>(a.mlp)[i];
+  const int4 u = a.units[blockIdx.x];
+  const int r = u.x, c = a.colour;
+  const RepDev &R = a.reps[r];
+  const RepState *S = a.st + r;
+  const int npp = R.hp * R.ny;
+  const bool valid = u.y + (int)threadIdx.x < npp;
+  const int p = valid ? u.y + (int)threadIdx.x : npp - 1;  // lanes past the plane shadow the last pair
+  March m;
+  march_init<MASK>(a, R, c, p, u.z, m);
+  const int nz = R.nz, nx = R.nx;
+  const bool zper = R.zb == BOUND_PERIODIC;
+  const int kb = u.z, ke = u.z + u.w;
+  unsigned acc = 0;
+  float qs[kQ];
+#pragma unroll
+  for (int q = 0; q < kQ; q++) qs[q] = 0.f;
+  __syncthreads();  // weights in shared memory
+  grid_dependency_wait();
+  const unsigned long long sw = S->sweep;
+  const float T = S->T, invT = 1.0f / S->T;
+  OPair om, o0, op;
+  const bool zm0 = kb > 0 || zper;
+  {
+    const int wrap = kb == 0 ? nz : 0;
+    load_opair_at<MASK>(m, m.off + (wrap - 1) * m.dz, m.offp + (wrap - 1) * m.dzp, zm0, om);
+    load_opair_at<MASK>(m, m.off, m.offp, true, o0);
+  }
+  bool zm = zm0;
+  auto wt = [&](float ee, uint8_t pp) { return MASK ? (ee != 0.f && pp != 0 ? 1.f : 0.f) : ee; };
+#pragma unroll 1
+  for (int k = kb; k < ke; k++) {
+    const bool zp = k + 1 < nz || zper;
+    const int up = k + 1 < nz ? 1 : 1 - nz;
+    load_opair_at<MASK>(m, m.off + up * m.dz, m.offp + up * m.dzp, zp, op);
+    float2 ax = *reinterpret_cast<const float2 *>(m.A0 + m.off);
+    float2 ay = *reinterpret_cast<const float2 *>(m.A1 + m.off);
+    float2 az = *reinterpret_cast<const float2 *>(m.A2 + m.off);
+    const int dx = m.s ? m.dx1 : m.dx0;
+    const float exv[3] = {__ldg(m.O0 + m.off + dx), __ldg(m.O1 + m.off + dx), __ldg(m.O2 + m.off + dx)};
+    OPair yp, ym;
+    load_opair_at<MASK>(m, m.off + m.dyp, m.offp + m.dypp, true, yp);
+    load_opair_at<MASK>(m, m.off + m.dym, m.offp + m.dymp, true, ym);
+    uint16_t pself = 0x0101;
+    uint8_t pex = 1;
+    if (MASK) {
+      pself = __ldg(reinterpret_cast<const uint16_t *>(m.PA + m.offp));
+      pex = __ldg(m.PO + m.offp + dx);
+    }
+    const int s = m.s;
+    const float exe = s ? m.ee1 : m.ee0;
+    const float erz[4] = {m.eyp, m.eym, zp ? 1.f : 0.f, zm ? 1.f : 0.f};
+    const OPair *rows4[4] = {&yp, &ym, &op, &om};
+    const uint8_t lo = (uint8_t)(o0.pt & 0xFF), hi = (uint8_t)(o0.pt >> 8);
+    // neighbour slots x+ x- y+ y- z+ z- of both sites (as update_pair)
+    float nbA[6][3], wA[6], eA[6], nbB[6][3], wB[6], eB[6];
+    if (s == 0) {
+      nbA[0][0] = o0.v[0].x; nbA[0][1] = o0.v[1].x; nbA[0][2] = o0.v[2].x; eA[0] = 1.f; wA[0] = wt(1.f, lo);
+      nbA[1][0] = exv[0]; nbA[1][1] = exv[1]; nbA[1][2] = exv[2]; eA[1] = exe; wA[1] = wt(exe, pex);
+      nbB[0][0] = o0.v[0].y; nbB[0][1] = o0.v[1].y; nbB[0][2] = o0.v[2].y; eB[0] = 1.f; wB[0] = wt(1.f, hi);
+      nbB[1][0] = o0.v[0].x; nbB[1][1] = o0.v[1].x; nbB[1][2] = o0.v[2].x; eB[1] = 1.f; wB[1] = wt(1.f, lo);
+    } else {
+      if (m.hasB) {
+        nbA[0][0] = o0.v[0].y; nbA[0][1] = o0.v[1].y; nbA[0][2] = o0.v[2].y; eA[0] = 1.f; wA[0] = wt(1.f, hi);
+      } else {
+        nbA[0][0] = exv[0]; nbA[0][1] = exv[1]; nbA[0][2] = exv[2]; eA[0] = exe; wA[0] = wt(exe, pex);
+      }
+      nbA[1][0] = o0.v[0].x; nbA[1][1] = o0.v[1].x; nbA[1][2] = o0.v[2].x; eA[1] = 1.f; wA[1] = wt(1.f, lo);
+      nbB[0][0] = exv[0]; nbB[0][1] = exv[1]; nbB[0][2] = exv[2]; eB[0] = exe; wB[0] = wt(exe, pex);
+      nbB[1][0] = o0.v[0].y; nbB[1][1] = o0.v[1].y; nbB[1][2] = o0.v[2].y; eB[1] = 1.f; wB[1] = wt(1.f, hi);
+    }
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      const OPair &o = *rows4[q];
+      nbA[2 + q][0] = o.v[0].x; nbA[2 + q][1] = o.v[1].x; nbA[2 + q][2] = o.v[2].x;
+      nbB[2 + q][0] = o.v[0].y; nbB[2 + q][1] = o.v[1].y; nbB[2 + q][2] = o.v[2].y;
+      eA[2 + q] = eB[2 + q] = erz[q];
+      wA[2 + q] = wt(erz[q], MASK ? (uint8_t)(o.pt & 0xFF) : 1);
+      wB[2 + q] = wt(erz[q], MASK ? (uint8_t)(o.pt >> 8) : 1);
+    }
+    const int psA = MASK ? (pself & 0xFF) : 1, psB = MASK ? (pself >> 8) : 1;
+    // the network for the warp's 64 sites
+    __syncwarp();
+    write_features(X + (size_t)(2 * lane) * kXs, nbA, wA, T, valid);
+    write_features(X + (size_t)(2 * lane + 1) * kXs, nbB, wB, T, valid && m.hasB);
+    __syncwarp();
+    mlp_warp(W, X, Y);
+    __syncwarp();
+    if (valid) {
+      float yA[4], yB[4];
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        yA[q] = Y[(2 * lane) * 4 + q];
+        yB[q] = Y[(2 * lane + 1) * 4 + q];
+      }
+      {
+        float sx = 0.f, sy = 0.f, sz = 0.f;
+        if (MASK && psA > 1) {
+          const float *nsb = a.ns + R.ns_off + (long long)(c * 3) * R.plane + m.off;
+          sx = __ldg(nsb);
+          sy = __ldg(nsb + R.plane);
+          sz = __ldg(nsb + 2 * R.plane);
+        }
+        const uint32_t nat = (uint32_t)(2 * m.h0 + s) + (uint32_t)nx * (uint32_t)m.row;
+        acc += site_update_learned<POT, MASK, FIELD, MODE>(R, a, c, ax.x, ay.x, az.x, nbA, wA, eA, psA, sx, sy, sz,
+                                                           yA, invT, nat, sw, qs);
+      }
+      if (m.hasB) {
+        float sx = 0.f, sy = 0.f, sz = 0.f;
+        if (MASK && psB > 1) {
+          const float *nsb = a.ns + R.ns_off + (long long)(c * 3) * R.plane + m.off + 1;
+          sx = __ldg(nsb);
+          sy = __ldg(nsb + R.plane);
+          sz = __ldg(nsb + 2 * R.plane);
+        }
+        const uint32_t nat = (uint32_t)(2 * m.h0 + 2 + s) + (uint32_t)nx * (uint32_t)m.row;
+        acc += site_update_learned<POT, MASK, FIELD, MODE>(R, a, c, ax.y, ay.y, az.y, nbB, wB, eB, psB, sx, sy, sz,
+                                                           yB, invT, nat, sw, qs);
+      }
+      *reinterpret_cast<float2 *>(m.A0 + m.off) = ax;
+      *reinterpret_cast<float2 *>(m.A1 + m.off) = ay;
+      *reinterpret_cast<float2 *>(m.A2 + m.off) = az;
+    }
+    om = o0;
+    o0 = op;
+    zm = true;
+    m.off += m.dz;
+    m.offp += m.dzp;
+    m.pid += m.dpid;
+    m.row += R.ny;
+    m.s ^= 1;
+  }
+  grid_launch_dependents();
+  flush_replica<kLPB, MODE>(a, r, 1, (unsigned)R.lcta, acc, qs, MASK);
+}
+
+template <int POT, bool MASK, bool FIELD>
+static const void *lmarch_fn(int mode) {
+  return mode == MODE_SWEEP_MEASURE ? (const void *)k_lmarch<POT, MASK, FIELD, MODE_SWEEP_MEASURE>
+                                    : (const void *)k_lmarch<POT, MASK, FIELD, MODE_SWEEP>;
+}
+
+static const void *lmarch_kernel(const Variant &v, int mode) {
+  if (v.pot == POT_LL) {
+    if (v.mask) return v.field ? lmarch_fn<POT_LL, true, true>(mode) : lmarch_fn<POT_LL, true, false>(mode);
+    return v.field ? lmarch_fn<POT_LL, false, true>(mode) : lmarch_fn<POT_LL, false, false>(mode);
+  }
+  if (v.mask) return v.field ? lmarch_fn<POT_GHRL, true, true>(mode) : lmarch_fn<POT_GHRL, true, false>(mode);
+  return v.field ? lmarch_fn<POT_GHRL, false, true>(mode) : lmarch_fn<POT_GHRL, false, false>(mode);
+}
+
+int lmarch_block_threads() { return kLPB; }
+
+bool lmarch_prepare(const Variant &v) {
+  if (v.pot == POT_PEAR) return false;
+  for (int mode : {MODE_SWEEP, MODE_SWEEP_MEASURE})
+    if (cudaFuncSetAttribute(lmarch_kernel(v, mode), cudaFuncAttributeMaxDynamicSharedMemorySize, kLmarchSmem) !=
+        cudaSuccess)
+      return false;
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, lmarch_kernel(v, MODE_SWEEP), kLPB, kLmarchSmem) !=
+      cudaSuccess)
+    return false;
+  return n > 0;
+}
+
+void launch_lmarch(const Variant &v, int mode, const PassArgs &a, bool pdl, cudaStream_t st) {
+  if (v.pot == POT_PEAR) return;  // the learned proposal is refused for Pear
+  PassArgs args = a;
+  void *params[] = {&args};
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(a.nunits);
+  cfg.blockDim = dim3(kLPB);
+  cfg.dynamicSmemBytes = kLmarchSmem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = pdl ? 1 : 0;
+  cudaLaunchKernelExC(&cfg, lmarch_kernel(v, mode), params);
+}
+
+}  // namespace mcx

@@ -698,7 +698,10 @@ constexpr int kLearnSmem = kMlpBytes + (kPB / 32) * (64 * kXs * 2 + 64 * 4 * 4);
 // The learned pass is bound by arithmetic, not by loads: it keeps one stage
 // (no prefetch of the next pair) so that three CTAs fit on an SM.
 template <int POT, bool MASK, bool FIELD, int MODE, bool LEARN>
-__global__ void __launch_bounds__(kPB, LEARN ? 3 : MCX_PASS_MIN_BLOCKS) k_pass(PassArgs a) {
+#ifndef MCX_LEARN_MIN_BLOCKS
+#define MCX_LEARN_MIN_BLOCKS 3
+#endif
+__global__ void __launch_bounds__(kPB, LEARN ? MCX_LEARN_MIN_BLOCKS : MCX_PASS_MIN_BLOCKS) k_pass(PassArgs a) {
   __shared__ PairStage<MASK> stages[LEARN ? 1 : 2];
   extern __shared__ __align__(16) uint8_t dyn_smem[];
   const int c = a.colour;

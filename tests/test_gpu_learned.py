@@ -117,3 +117,25 @@ def test_learned_chain_samples_the_same_equilibrium(T):
         a, b = res["plain"][q], res["vmf_mlp"][q]
         se = np.sqrt(a.var(ddof=1) / len(a) + b.var(ddof=1) / len(b))
         assert abs(a.mean() - b.mean()) < 4 * se + 1e-4, (q, a.mean(), b.mean(), se)
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_learned_march_equals_learned_direct_pass(name):
+    """The learned z-march and the learned direct pass give bit-identical
+    states, step sizes and acceptance counts after measured sweeps."""
+    m = CASES[name]
+    params = _weights(4)
+    lat = O.Lattice(m)
+    out = []
+    for kind in ("march", "direct"):
+        with mcx.Engine([desc_from_model(m, T=0.9, seed=13, stream=2)]) as eng:
+            eng.pass_kind = kind
+            eng.set_state(0, random_state(m, lat.pt, np.random.default_rng(6)))
+            eng.set_mlp(M.pack_weights(params))
+            eng.set_proposal("vmf_mlp")
+            eng.sweep(11, measure=True)
+            out.append((eng.get_state(0), eng.stats(0)))
+    (sa, ta), (sb, tb) = out
+    assert np.array_equal(sa, sb)
+    assert ta[mcx.ST_ANG_VAR] == tb[mcx.ST_ANG_VAR] and ta[mcx.ST_ACC] == tb[mcx.ST_ACC]
+    assert ta[mcx.ST_S1] == pytest.approx(tb[mcx.ST_S1], rel=1e-6)
