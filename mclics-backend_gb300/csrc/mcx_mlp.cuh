@@ -81,6 +81,21 @@ __device__ __forceinline__ uint32_t gelu_bf16x2(float a, float b) {
 
 __device__ __forceinline__ uint32_t lds32(const uint8_t *p) { return *reinterpret_cast<const uint32_t *>(p); }
 
+// B fragments of two adjacent n-tiles for one 16-wide k-tile, from a
+// transposed weight block (row n holds the k values): four 8x8 matrices, rows
+// n0..n0+7 at k and k+8, rows n0+8..n0+15 at k and k+8.  Lane l supplies the
+// row address of matrix l/8; the result is {b0, b1} of n-tile n0/8 and of the
+// next one, exactly the words two LDS.32 per fragment would read.
+__device__ __forceinline__ void ldsm_b2(const uint8_t *wt, int stride_elems, int n0, int k0, uint32_t b[4]) {
+  const int lane = threadIdx.x & 31;
+  const int row = n0 + (lane & 7) + ((lane >> 4) << 3);
+  const int col = k0 + (((lane >> 3) & 1) << 3);
+  const uint32_t addr = (uint32_t)__cvta_generic_to_shared(wt + ((size_t)row * stride_elems + col) * 2);
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];"
+               : "=r"(b[0]), "=r"(b[1]), "=r"(b[2]), "=r"(b[3])
+               : "r"(addr));
+}
+
 // The network for 64 rows of X (bf16, row stride kXs) -> Y (64 x 4 floats),
 // by one warp.  Rows are sites; all 32 lanes must call.
 __device__ __forceinline__ void mlp_warp(const uint8_t *W, const __nv_bfloat16 *X, float *Y) {
@@ -113,11 +128,13 @@ __device__ __forceinline__ void mlp_warp(const uint8_t *W, const __nv_bfloat16 *
         h[half][1] = bb1;
         h[half][2] = bb0;
         h[half][3] = bb1;
+      }
 #pragma unroll
-        for (int kt = 0; kt < 2; kt++) {
-          const uint8_t *wr = W1 + ((nt * 8 + g) * kW1s + kt * 16 + 2 * tg) * 2;
-          mma_bf16(h[half], a1[kt], lds32(wr), lds32(wr + 16));
-        }
+      for (int kt = 0; kt < 2; kt++) {
+        uint32_t bf[4];
+        ldsm_b2(W1, kW1s, 16 * q, kt * 16, bf);
+        mma_bf16(h[0], a1[kt], bf[0], bf[1]);
+        mma_bf16(h[1], a1[kt], bf[2], bf[3]);
       }
       a2[q][0] = gelu_bf16x2(h[0][0], h[0][1]);
       a2[q][1] = gelu_bf16x2(h[0][2], h[0][3]);
@@ -137,11 +154,13 @@ __device__ __forceinline__ void mlp_warp(const uint8_t *W, const __nv_bfloat16 *
         h[half][1] = bb1;
         h[half][2] = bb0;
         h[half][3] = bb1;
+      }
 #pragma unroll
-        for (int kt = 0; kt < 4; kt++) {
-          const uint8_t *wr = W2 + ((nt * 8 + g) * kW2s + kt * 16 + 2 * tg) * 2;
-          mma_bf16(h[half], a2[kt], lds32(wr), lds32(wr + 16));
-        }
+      for (int kt = 0; kt < 4; kt++) {
+        uint32_t bf[4];
+        ldsm_b2(W2, kW2s, 16 * q, kt * 16, bf);
+        mma_bf16(h[0], a2[kt], bf[0], bf[1]);
+        mma_bf16(h[1], a2[kt], bf[2], bf[3]);
       }
       uint32_t a3[4];
       a3[0] = gelu_bf16x2(h[0][0], h[0][1]);

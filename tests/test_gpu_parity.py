@@ -47,6 +47,7 @@ CASES = {
                               surfaces=[O.Surface("fg_ghrl", 1.5), O.Surface("rp_ghrl", 2.0, 20, 70)]),
     "custom_mixed": _custom_model(),
     "bulk_ll_x_periodic_yz_free": O.Model(nx=14, ny=5, nz=3, xbound="periodic", ybound="free", zbound="free"),
+    "tiny_ll_nx2": O.Model(nx=2, ny=4, nz=6, potential="ll", A=1.1),
     "bulk_pear_field": O.Model(nx=12, ny=8, nz=6, potential="pear", A=1.0, B1=0.3, C=0.3, elecA=0.4, elecZ=1.0,
                                elecE=1.0),
     "sphere_pear_homeotropic": O.Model(nx=12, ny=12, nz=12, geometry="sphere", potential="pear", B1=0.3, C=0.3,
