@@ -255,6 +255,9 @@ def main():
     ap.add_argument("--replicas", type=int, default=1,
                     help="independent lattices in one engine (default 1, the headline workload; more for profiling "
                          "the batched pass)")
+    ap.add_argument("--pass-shape", default=None,
+                    help="KIND:BLOCK:PLANES (e.g. march:256:0) instead of the autotuner's choice; for profiling "
+                         "runs, where a profiler's serialisation would distort the autotuner's timings")
     ap.add_argument("--proposal", default="plain", choices=["plain", "vmf_mlp"],
                     help="plain (the reference's move; default) or the learned proposal with untrained weights "
                          "(for profiling its pass)")
@@ -289,7 +292,13 @@ def main():
     # the state, before anything is timed)
     for q in range(R):
         eng.init_homogeneous(q, 0.0, 0.0)
-    tuned = eng.autotune()
+    if args.pass_shape:
+        kind, blk, planes = args.pass_shape.split(":")
+        eng.pass_kind = kind
+        eng.set_march_shape(int(blk), int(planes))
+        tuned = (int(blk), int(planes), None)
+    else:
+        tuned = eng.autotune()
     if args.proposal != "plain":
         from mcx import gain
         eng.set_mlp(gain.init_weights(1))
