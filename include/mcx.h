@@ -396,6 +396,32 @@ mcx_status mcx_load(mcx_engine *eng, const char *path);
 mcx_status mcx_exchange(mcx_engine *eng, int n_pairs, const int *pairs, unsigned int seed, unsigned long long round,
                         int *accepted);
 
+/* mcx_combine_stats() output layout (MCX_COMBINED_LEN doubles). */
+enum {
+  MCX_CB_T = 0,        /* mean temperature of the combined replicas */
+  MCX_CB_S = 1,        /* mean over replicas of their po.dat S */
+  MCX_CB_VAR_S = 2,    /* mean of their varS + variance (ddof 0) of their S */
+  MCX_CB_E = 3,        /* the same for E */
+  MCX_CB_VAR_E = 4,
+  MCX_CB_P = 5,        /* mean polarization of the current states (Pear), else NaN */
+  MCX_CB_N = 6,        /* replicas combined */
+  MCX_CB_T_SPREAD = 7  /* largest minus smallest temperature */
+};
+#define MCX_COMBINED_LEN 8
+
+/* Combines independent replicas into one po.dat row on the GPU, the way
+ * average_replicas.py:74-103 combines po.dat files of runs that differ only in
+ * their seed: each replica's row is S = S1/N, varS = S2/N - S^2, E and varE
+ * likewise (the columns of src/evolve_thermal.cpp:78-86 over its measured
+ * sweeps); the combined row is the mean S, the law-of-total-variance
+ * mean(varS) + var(S) and the same for E, and for Pear replicas the mean
+ * polarization.  replicas: n indices (NULL with n <= 0: every replica).
+ * Errors (MCX_ERR_INVALID): a replica without measured sweeps; Pear mixed
+ * with other potentials (the script's differing column counts); temperatures
+ * more than 1e-3 apart (a point the script skips) -- out is filled in that
+ * last case, so the caller can see the spread. */
+mcx_status mcx_combine_stats(mcx_engine *eng, int n, const int *replicas, double *out /* MCX_COMBINED_LEN */);
+
 /* ./mc_sim <param_file> (src/main.cpp:63-83): reads the reference's parameter
  * file (src/io.cpp:81-253), runs the selected mode on the GPU and writes
  * po.dat and director_field_*.csv into out_dir (NULL: current directory). */

@@ -1401,6 +1401,58 @@ extern "C" mcx_status mcx_exchange(mcx_engine *e, int n, const int *pairs, unsig
   return MCX_OK;
 }
 
+extern "C" mcx_status mcx_combine_stats(mcx_engine *e, int n, const int *replicas, double *out) {
+  if (!e) return fail(nullptr, MCX_ERR_INVALID, "null engine");
+  if (!out) return fail(e, MCX_ERR_INVALID, "mcx_combine_stats: null output");
+  std::vector<int> idx;
+  if (n <= 0 || !replicas) {
+    if (n > 0) return fail(e, MCX_ERR_INVALID, "mcx_combine_stats: null replica list");
+    for (int q = 0; q < e->nrep; q++) idx.push_back(q);
+  } else {
+    idx.assign(replicas, replicas + n);
+  }
+  int pear = 0;
+  for (int r : idx) {
+    if (mcx_status st = check_rep(e, r)) return st;
+    pear += e->desc[r].potential == MCX_POT_PEAR;
+  }
+  const int m = (int)idx.size();
+  if (pear != 0 && pear != m)
+    return fail(e, MCX_ERR_INVALID, "mcx_combine_stats: Pear replicas mixed with other potentials");
+  if (mcx_status st = flush(e)) return st;
+  // scratch: the index list, then 3 director sums per replica (Pear), then the output
+  const size_t pol_off = ((size_t)m * sizeof(int) + 15) / 16 * 16;
+  const size_t out_off = pol_off + (pear ? (size_t)m * 3 * sizeof(double) : 0);
+  char *scratch = nullptr;
+  CK(e, cudaMallocAsync((void **)&scratch, out_off + 16 * sizeof(double), e->stream));
+  struct Free {
+    mcx_engine *e;
+    char *p;
+    ~Free() { cudaFreeAsync(p, e->stream); }
+  } guard{e, scratch};
+  int *d_idx = (int *)scratch;
+  double *d_pol = pear ? (double *)(scratch + pol_off) : nullptr;
+  double *d_out = (double *)(scratch + out_off);
+  CK(e, cudaMemcpyAsync(d_idx, idx.data(), (size_t)m * sizeof(int), cudaMemcpyHostToDevice, e->stream));
+  for (int i = 0; pear && i < m; i++) {
+    launch_polarization(e->rep[idx[i]], e->d_dir, d_pol + 3 * (size_t)i, e->stream);
+    e->launches++;
+  }
+  launch_combine(e->d_rep, e->d_st, e->d_stats, d_pol, d_idx, m, d_out, e->stream);
+  e->launches++;
+  CKL(e);
+  double h[MCX_COMBINED_LEN + 1];
+  CK(e, cudaMemcpyAsync(h, d_out, sizeof h, cudaMemcpyDeviceToHost, e->stream));
+  CK(e, cudaStreamSynchronize(e->stream));
+  if (h[MCX_COMBINED_LEN] > 0)
+    return fail(e, MCX_ERR_INVALID, "mcx_combine_stats: %d replica(s) without measured sweeps",
+                (int)h[MCX_COMBINED_LEN]);
+  memcpy(out, h, sizeof(double) * MCX_COMBINED_LEN);
+  if (h[MCX_CB_T_SPREAD] > 1e-3)
+    return fail(e, MCX_ERR_INVALID, "mcx_combine_stats: temperatures differ by %g (> 1e-3)", h[MCX_CB_T_SPREAD]);
+  return MCX_OK;
+}
+
 extern "C" mcx_status mcx_measure(mcx_engine *e, int r, double *out) {
   if (mcx_status st = check_rep(e, r)) return st;
   if (!out) return fail(e, MCX_ERR_INVALID, "null output");

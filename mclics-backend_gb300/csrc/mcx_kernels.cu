@@ -873,6 +873,106 @@ void launch_polarization(const RepDev &R, const float *dir, double *out, cudaStr
   k_polarization<<<256, 256, 0, st>>>(R, dir, out);
 }
 
+// Replica combination (average_replicas.py:74-103).  One CTA; every thread
+// walks the index list with a fixed stride and the partial sums meet in a
+// fixed-order tree, so the result does not depend on timing.  Pass 1 sums T,
+// S, varS, E, varE and P and finds the T range; pass 2 sums the squared
+// deviations of S and E from their means (numpy's var with ddof 0).
+// pol: three FP64 director sums per listed replica, or null.
+constexpr int kCombineThreads = 256;
+
+struct CombineRow {
+  double S, vS, E, vE;
+};
+
+__device__ __forceinline__ CombineRow combine_row(const double *st) {
+  const double n = st[0];
+  const double S = st[1] / n, E = st[3] / n;
+  return {S, st[2] / n - S * S, E, st[4] / n - E * E};
+}
+
+template <int K>
+__device__ __forceinline__ void block_sum(double (&v)[K], double (*red)[kCombineThreads]) {
+  for (int q = 0; q < K; q++) red[q][threadIdx.x] = v[q];
+  __syncthreads();
+  for (int w = kCombineThreads / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w)
+      for (int q = 0; q < K; q++) red[q][threadIdx.x] += red[q][threadIdx.x + w];
+    __syncthreads();
+  }
+  for (int q = 0; q < K; q++) v[q] = red[q][0];
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(kCombineThreads) k_combine(const RepDev *rep, const RepState *rst,
+                                                             const double *stats, const double *pol,
+                                                             const int *idx, int n, double *out) {
+  __shared__ double red[6][kCombineThreads];
+  __shared__ float tmin[kCombineThreads], tmax[kCombineThreads];
+  __shared__ int empty[kCombineThreads];
+  double v[6] = {0, 0, 0, 0, 0, 0};  // T, S, varS, E, varE, P
+  float lo = INFINITY, hi = -INFINITY;
+  int ne = 0;
+  for (int i = threadIdx.x; i < n; i += kCombineThreads) {
+    const int r = idx[i];
+    const double *st = stats + (size_t)r * kStats;
+    const float T = rst[r].T;
+    lo = fminf(lo, T);
+    hi = fmaxf(hi, T);
+    v[0] += (double)T;
+    if (st[0] <= 0) {
+      ne++;
+      continue;
+    }
+    const CombineRow c = combine_row(st);
+    v[1] += c.S;
+    v[2] += c.vS;
+    v[3] += c.E;
+    v[4] += c.vE;
+    if (pol) {
+      const double *p = pol + 3 * (size_t)i;
+      v[5] += sqrt(p[0] * p[0] + p[1] * p[1] + p[2] * p[2]) / (double)rep[r].ntot;
+    }
+  }
+  tmin[threadIdx.x] = lo;
+  tmax[threadIdx.x] = hi;
+  empty[threadIdx.x] = ne;
+  block_sum(v, red);  // its barriers also publish tmin/tmax/empty
+  if (threadIdx.x == 0)
+    for (int t = 1; t < kCombineThreads; t++) {
+      lo = fminf(lo, tmin[t]);
+      hi = fmaxf(hi, tmax[t]);
+      ne += empty[t];
+    }
+  const double inv = 1.0 / (double)n;
+  const double mS = v[1] * inv, mE = v[3] * inv;
+  double d[2] = {0, 0};
+  for (int i = threadIdx.x; i < n; i += kCombineThreads) {
+    const double *st = stats + (size_t)idx[i] * kStats;
+    if (st[0] <= 0) continue;
+    const CombineRow c = combine_row(st);
+    d[0] += (c.S - mS) * (c.S - mS);
+    d[1] += (c.E - mE) * (c.E - mE);
+  }
+  block_sum(d, red);
+  if (threadIdx.x == 0) {
+    out[0] = v[0] * inv;
+    out[1] = mS;
+    out[2] = v[2] * inv + d[0] * inv;
+    out[3] = mE;
+    out[4] = v[4] * inv + d[1] * inv;
+    out[5] = pol ? v[5] * inv : __longlong_as_double(0x7ff8000000000000LL);
+    out[6] = (double)n;
+    out[7] = (double)hi - (double)lo;
+    out[8] = (double)ne;
+  }
+}
+
+void launch_combine(const RepDev *rep, const RepState *st, const double *stats, const double *pol, const int *idx,
+                    int n, double *out, cudaStream_t s) {
+  k_combine<<<1, kCombineThreads, 0, s>>>(rep, st, stats, pol, idx, n, out);
+}
+
 void launch_local_order(const RepDev &R, const float *dir, const uint8_t *pt, float *out, cudaStream_t st) {
   k_local_order<<<(unsigned)((R.ntot + 255) / 256), 256, 0, st>>>(R, dir, pt, out);
 }

@@ -113,6 +113,10 @@ void launch_init(const RepDev &R, const uint8_t *pt, float *dir, int mode, uint3
                  cudaStream_t st);
 // Sum of every site's director (3 doubles at out).
 void launch_polarization(const RepDev &R, const float *dir, double *out, cudaStream_t st);
+// out: the MCX_COMBINED_LEN doubles of mcx_combine_stats, then the count of
+// listed replicas without measured sweeps.
+void launch_combine(const RepDev *rep, const RepState *st, const double *stats, const double *pol, const int *idx,
+                    int n, double *out, cudaStream_t s);
 // Per-site local order parameter (natural order; NaN at inactive sites).
 void launch_local_order(const RepDev &R, const float *dir, const uint8_t *pt, float *out, cudaStream_t st);
 

@@ -306,9 +306,15 @@ mcx_status run(const char *path, const char *out_dir) {
     check(mcx_get_mask(e, 0, pt.data(), ns.data()));
     check(mcx_get_state(e, 0, ni.data()));
     write_snapshot(dir + "ic.csv", ni, pt, descs[0], nullptr);
-    std::vector<FILE *> po(R, nullptr);
-    for (int r = 0; r < R; r++) {
-      std::string name = r == 0 ? dir + "po.dat" : dir + "po_r" + std::to_string(r) + ".dat";
+    // po.dat per replica (po_r<r>.dat for r > 0) and, with several replicas,
+    // po_avg.dat: their combination by mcx_combine_stats, the table
+    // average_replicas.py would write from those files
+    const int nfiles = R > 1 ? R + 1 : 1;
+    std::vector<FILE *> po(nfiles, nullptr);
+    for (int r = 0; r < nfiles; r++) {
+      std::string name = r == 0 ? dir + "po.dat"
+                         : r == R ? dir + "po_avg.dat"
+                                  : dir + "po_r" + std::to_string(r) + ".dat";
       po[r] = fopen(name.c_str(), "a");
       if (!po[r]) {
         g_err = "cannot open " + name;
@@ -351,6 +357,19 @@ mcx_status run(const char *path, const char *out_dir) {
         }
         fprintf(po[r], "\n");
         fflush(po[r]);
+      }
+      if (R > 1) {
+        double cb[MCX_COMBINED_LEN];
+        check(mcx_combine_stats(e, 0, nullptr, cb));
+        FILE *f = po[R];
+        if (label_fmt[1] == 'd')
+          fprintf(f, "%d", ilabel);
+        else
+          fprintf(f, "%g", label);
+        fprintf(f, " %g %g %g %g", cb[MCX_CB_S], cb[MCX_CB_VAR_S], cb[MCX_CB_E], cb[MCX_CB_VAR_E]);
+        if (descs[0].potential == MCX_POT_PEAR) fprintf(f, " %g", cb[MCX_CB_P]);
+        fprintf(f, "\n");
+        fflush(f);
       }
       if (!snap.empty()) {
         check(mcx_get_state(e, 0, ni.data()));

@@ -41,6 +41,9 @@ STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "out of memory", 4
 M_E, M_E_VALID, M_Q, M_S, M_DIRECTOR, M_VALID = 0, 1, 2, 11, 12, 15
 ST_N, ST_S1, ST_S2, ST_E1, ST_E2, ST_EV1, ST_EV2, ST_ACC, ST_SWEEPS, ST_LAST_E, ST_LAST_S, ST_ANG_VAR, ST_SWEEP_INDEX = \
     range(13)
+# mcx_combine_stats layout
+CB_T, CB_S, CB_VAR_S, CB_E, CB_VAR_E, CB_P, CB_N, CB_T_SPREAD = range(8)
+COMBINED_LEN = 8
 
 
 class McxError(RuntimeError):
@@ -157,6 +160,7 @@ def lib() -> C.CDLL:
         L.mcx_save.argtypes = [V, C.c_char_p]
         L.mcx_load.argtypes = [V, C.c_char_p]
         L.mcx_exchange.argtypes = [V, I, V, C.c_uint, C.c_ulonglong, V]
+        L.mcx_combine_stats.argtypes = [V, I, V, V]
         L.mcx_set_mlp.argtypes = [V, V, I]
         L.mcx_get_mlp.argtypes = [V, V]
         L.mcx_set_proposal.argtypes = [V, I]
@@ -372,6 +376,19 @@ class Engine:
         acc = np.zeros(len(pr), np.int32)
         self._ck(self._L.mcx_exchange(self._h, len(pr), _p(pr), int(seed) & 0xFFFFFFFF, int(round), _p(acc)))
         return acc
+
+    def combine_stats(self, replicas=None) -> dict:
+        """One po.dat row combining independent replicas (all when None) by the
+        law of total variance, on the GPU: T, S, varS, E, varE and, for Pear,
+        P (NaN otherwise)."""
+        out = np.zeros(COMBINED_LEN, np.float64)
+        if replicas is None:
+            self._ck(self._L.mcx_combine_stats(self._h, 0, None, _p(out)))
+        else:
+            idx = np.ascontiguousarray(replicas, np.int32).ravel()
+            self._ck(self._L.mcx_combine_stats(self._h, len(idx), _p(idx), _p(out)))
+        return {"T": out[CB_T], "S": out[CB_S], "varS": out[CB_VAR_S], "E": out[CB_E], "varE": out[CB_VAR_E],
+                "P": out[CB_P], "n": int(out[CB_N]), "T_spread": out[CB_T_SPREAD]}
 
     @property
     def pass_kind(self) -> str:

@@ -21,7 +21,7 @@ point types).  The full configurations run MCT = MCS = 1000; the defaults
 here time fewer sweeps per step so that a run takes seconds, which does not
 change the per-sweep cost.
 
-    PYTHONPATH=mclics-backend_gb300 python -m mcx.workloads c3 [--replicas 256] [--sweeps 50]
+    PYTHONPATH=mclics-backend_gb300 python -m mcx.workloads c3 [--replicas 256] [--sweeps 50] [--pass-shape march:64:16]
     PYTHONPATH=mclics-backend_gb300 python -m mcx.workloads c5 [--replicas 64] [--sweeps 20] [--proposal vmf_mlp]
 """
 from __future__ import annotations
@@ -76,13 +76,24 @@ def _time_blocks(eng, steps, mct, mcs, per_step=None):
     return time.perf_counter() - t0
 
 
-def run_c3(replicas=256, sweeps=50, steps=3, seed=3):
+def _shape(eng, pass_shape):
+    """The autotuner's pass shape, or KIND:BLOCK:PLANES as given (profiling
+    runs, where a profiler's serialisation would distort the autotuner)."""
+    if not pass_shape:
+        return eng.autotune()
+    kind, blk, planes = pass_shape.split(":")
+    eng.pass_kind = kind
+    eng.set_march_shape(int(blk), int(planes))
+    return int(blk), int(planes), None
+
+
+def run_c3(replicas=256, sweeps=50, steps=3, seed=3, pass_shape=None):
     descs = c3_descs(replicas, seed)
     sites = sum(d.nx * d.ny * d.nz for d in descs)
     with Engine(descs) as eng:
         for q in range(replicas):
             eng.init_random(q, 7 + q)
-        tuned = eng.autotune()
+        tuned = _shape(eng, pass_shape)
         _time_blocks(eng, 1, sweeps, sweeps)  # warm-up: graphs built
         dt = _time_blocks(eng, steps, sweeps, sweeps)
         sw_ms = None
@@ -97,7 +108,8 @@ def run_c3(replicas=256, sweeps=50, steps=3, seed=3):
     ach = BYTES_PER_SITE_PASS_MASKED * sites / (sw_ms / 2 * 1e-3) / 1e9 if sw_ms else None
     return {"workload": "c3: GHRL slab batch", "replicas": replicas, "sites": int(sites),
             "sides": sorted(set(int(d.nx) for d in descs)), "site_updates_per_s": ups,
-            "sweep_ms": sw_ms, "pass_kernel": f"z-march {tuned[0]} x {tuned[1]} (autotuned)",
+            "sweep_ms": sw_ms,
+            "pass_kernel": f"z-march {tuned[0]} x {tuned[1]} ({'given' if pass_shape else 'autotuned'})",
             "roofline": {"achieved_gbs": ach, "peak_gbs": peak, "frac": ach / peak if ach else None,
                          "peak_source": src, "bytes_per_site_pass": BYTES_PER_SITE_PASS_MASKED},
             "mean_S": float(S)}
@@ -139,9 +151,11 @@ def main():
     ap.add_argument("--replicas", type=int, default=None)
     ap.add_argument("--sweeps", type=int, default=None)
     ap.add_argument("--proposal", default="plain", choices=["plain", "vmf_mlp"])
+    ap.add_argument("--steps", type=int, default=3, help="c3: timed blocks")
+    ap.add_argument("--pass-shape", default=None, help="c3: KIND:BLOCK:PLANES instead of the autotuner's choice")
     a = ap.parse_args()
     if a.which == "c3":
-        res = run_c3(replicas=a.replicas or 256, sweeps=a.sweeps or 50)
+        res = run_c3(replicas=a.replicas or 256, sweeps=a.sweeps or 50, steps=a.steps, pass_shape=a.pass_shape)
     else:
         res = run_c5(replicas=a.replicas or 64, sweeps=a.sweeps or 20, proposal=a.proposal)
     print(json.dumps(res), flush=True)

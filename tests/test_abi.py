@@ -119,7 +119,7 @@ def test_parser_reads_reference_sample_style(tmp_path):
     ("geometry slab\nanchoring_type 0 homeotropic\nW 0 1\n", 6, "define 2 boundaries"),
     ("geometry sphere\nanchoring_type 0 nonsense\nW 0 1\n", 6, "not defined"),
     ("geometry sphere\nanchoring_type 0 rp\nW 0 1\n", 6, "phi_s"),
-    ("potential pear\n", 4, "pear"),
+    ("potential gay_berne\n", 6, "ll | ghrl | pear"),
     ("Nx 15\n", 4, "even"),
     ("evol sideways\n", 6, "evol mode"),
     ("dT 0\n", 6, "dT"),

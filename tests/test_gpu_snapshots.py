@@ -8,7 +8,11 @@
 - mcx_exchange: the decisions are min(1, exp((1/Ta - 1/Tb)(Ha - Hb))) against
   the documented Philox uniform; accepted pairs swap T.
 - mcx_run_file: ./mc_sim on a small parameter file writes po.dat and the
-  director_field_*.csv snapshots in the reference's formats."""
+  director_field_*.csv snapshots in the reference's formats.
+- mcx_combine_stats: the GPU combination of replicas equals the oracle's
+  restatement of average_replicas.py applied to each replica's po.dat row;
+  with `replicas R` the driver's po_avg.dat equals the oracle's combination of
+  the po.dat files it wrote (to their %g rounding)."""
 import os
 
 import numpy as np
@@ -16,6 +20,7 @@ import pytest
 
 import mcx
 from oracle import oracle as O
+from oracle import replicas as OR
 from helpers import desc_from_model, random_state
 
 pytestmark = pytest.mark.gpu
@@ -189,3 +194,60 @@ def test_run_file_pear_adds_polarization(tmp_path):
     assert rows[0] == ["T", "S", "varS", "E", "varE", "P"]
     data = np.array(rows[1:], float)
     assert data.shape == (3, 6) and np.all((data[:, 5] >= 0) & (data[:, 5] <= 1))
+
+
+def _replica_rows(eng, idx, pear=False):
+    return [OR.po_row(float(eng.desc(r)[0].T), eng.stats(r), eng.polarization(r) if pear else None) for r in idx]
+
+
+def test_combine_stats_matches_oracle_combiner():
+    m = O.Model(nx=8, ny=8, nz=8, potential="ll")
+    descs = [desc_from_model(m, T=1.0, seed=40 + r, stream=r) for r in range(6)]
+    with mcx.Engine(descs) as eng:
+        for r in range(6):
+            eng.init_random(r, 90 + r)
+        eng.sweep(20)
+        eng.reset_stats()
+        eng.sweep(30, measure=True)
+        for idx in (list(range(6)), [0, 2, 5], [3]):
+            got = eng.combine_stats(None if len(idx) == 6 else idx)
+            want = OR.combine([[row] for row in _replica_rows(eng, idx)])[0]
+            assert got["n"] == len(idx) and np.isnan(got["P"])
+            np.testing.assert_allclose([got[k] for k in ("T", "S", "varS", "E", "varE")], want, rtol=1e-12)
+        # a replica without measured sweeps, and temperatures more than 1e-3 apart
+        eng.reset_stats(4)
+        with pytest.raises(mcx.McxError, match="without measured sweeps"):
+            eng.combine_stats()
+        eng.combine_stats([0, 1])
+        eng.set_temperature(1.01, 1)
+        with pytest.raises(mcx.McxError, match="temperatures differ"):
+            eng.combine_stats([0, 1])
+        with pytest.raises(mcx.McxError):
+            eng.combine_stats([0, 6])
+
+
+def test_combine_stats_pear_polarization():
+    m = O.Model(nx=8, ny=6, nz=10, potential="pear", B1=0.3, C=0.3)
+    descs = [desc_from_model(m, T=0.8, seed=7 + r, stream=r) for r in range(3)]
+    with mcx.Engine(descs) as eng:
+        for r in range(3):
+            eng.init_random(r, 5 + r)
+        eng.sweep(10)
+        eng.reset_stats()
+        eng.sweep(12, measure=True)
+        got = eng.combine_stats()
+        want = OR.combine([[row] for row in _replica_rows(eng, range(3), pear=True)])[0]
+    np.testing.assert_allclose([got[k] for k in ("T", "S", "varS", "E", "varE", "P")], want, rtol=1e-12)
+
+
+def test_run_file_replicas_writes_combined_table(tmp_path):
+    pf = tmp_path / "params.txt"
+    pf.write_text(PARAMS + "replicas  3\n")
+    mcx.run_file(str(pf), str(tmp_path) + "/")
+    files = ["po.dat", "po_r1.dat", "po_r2.dat"]
+    want = np.array(OR.combine([OR.read_po(str(tmp_path / f)) for f in files]))
+    lines = (tmp_path / "po_avg.dat").read_text().splitlines()
+    assert lines[0].split() == ["T", "S", "varS", "E", "varE"]
+    got = np.array([[float(x) for x in ln.split()] for ln in lines[1:]])
+    assert got.shape == want.shape == (3, 5)
+    np.testing.assert_allclose(got, want, rtol=1e-3, atol=1e-7)
