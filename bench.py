@@ -52,6 +52,13 @@ SITES = NX * NY * NZ
 TI, TF, DT = 1.20, 0.90, -0.01
 MCT = MCS = 2000
 BYTES_PER_SITE_PASS = 18
+# pass forms of the plain proposal: roofline kernel name, description
+FORMS = {"march": ("k_march<LL> (red/black pass)", "z-march"),
+         "march_async": ("k_amarch<LL> (red/black pass, cp.async prefetch)", "z-march with cp.async prefetch"),
+         "march_tma": ("k_tmarch<LL> (red/black pass, bulk-copy staged)", "z-march with bulk-copy staging"),
+         "march_persistent": ("k_pmarch<LL> (red/black passes, one cooperative launch)", "persistent z-march"),
+         "direct": ("k_pass<LL> (red/black pass)", "direct pass"),
+         "staged": ("k_tpass<LL> (red/black pass)", "staged pass")}
 WORKLOAD = ("LL bulk 128^3 periodic, A=1, homogeneous ic along z, anneal Ti=1.20 -> Tf=0.90 dT=-0.01, "
             "MCT=2000 MCS=2000 per temperature")
 
@@ -299,6 +306,7 @@ def main():
         tuned = (int(blk), int(planes), None)
     else:
         tuned = eng.autotune()
+    form, how = eng.pass_kind, "given" if args.pass_shape else "autotuned"
     if args.proposal != "plain":
         from mcx import gain
         eng.set_mlp(gain.init_weights(1))
@@ -440,17 +448,20 @@ def main():
                    "l2": "flushed (256 MiB write) between steps outside the timed windows; the 25 MB lattice "
                          "stays L2-resident within a step",
                    "parallelism": (f"replicas x{ws} ranks" if ws > 1 else "one GPU") + f", {R} lattice(s) per engine",
-                   "pass_kernel": ((f"z-march, {tuned[0]} threads x {tuned[1]} planes per CTA (autotuned)" if tuned[1] > 0
-                                    else f"z-march, {tuned[0]} threads x balanced chunks filling "
-                                         f"{max(1, -tuned[1])} wave(s) of resident CTAs (autotuned)")
-                                   if args.proposal == "plain" else "learned-proposal pass (k_pass, BF16 MLP)"),
+                   "pass_kernel": ((f"{FORMS[form][1]}, {tuned[0]} threads x {tuned[1]} planes per CTA ({how})"
+                                    if tuned[1] > 0
+                                    else f"{FORMS[form][1]}, {tuned[0]} threads x balanced chunks filling "
+                                         f"{max(1, -tuned[1])} wave(s) of resident CTAs ({how})")
+                                   if args.proposal == "plain" else "learned-proposal z-march (k_lmarch, BF16 MLP)"),
                    "S_E_last_step": [rows[-1][0], rows[-1][1], rows[-1][2]] if rows else None},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": traffic, "peak_source": peak_src, "kernel": "k_march<LL> (red/black pass)" if args.proposal == "plain" else "k_pass<LL, learned>",
+                     "traffic": traffic, "peak_source": peak_src, "kernel": FORMS[form][0] if args.proposal == "plain" else "k_lmarch<LL> (learned proposal)",
                      "bytes_per_launch": bytes_per_launch, "launch_ms": per_launch_ms,
                      "launch_ms_isolated": per_launch_isolated_ms,
-                     "launch_ms_method": "400 graph-replayed unmeasured sweeps between two CUDA events on the "
-                                         "engine stream / 800 pass launches (launch gaps included)",
+                     "launch_ms_method": ("400 unmeasured sweeps in cooperative launches between two CUDA events "
+                                          "on the engine stream / 800 passes" if form == "march_persistent" else
+                                          "400 graph-replayed unmeasured sweeps between two CUDA events on the "
+                                          "engine stream / 800 pass launches (launch gaps included)"),
                      "pass_share_of_sweep": pass_ms.value / all_ms.value if all_ms.value else None},
         "cpu_baseline": cpu,
         "e2e": e2e,

@@ -223,9 +223,23 @@ int mcx_get_staged(const mcx_engine *eng);
  *   MCX_PASS_STAGED  the staged TMA pass above (mcx_set_staged);
  *   MCX_PASS_MARCH_TMA  the z-march with each plane's rows brought into
  *                    shared memory by bulk copies one plane ahead (unmasked
- *                    batches only).
+ *                    batches only);
+ *   MCX_PASS_MARCH_ASYNC  the z-march with every thread copying its next
+ *                    plane's neighbourhood into shared memory by cp.async
+ *                    while it updates the current plane (unmasked LL and GHRL
+ *                    batches only);
+ *   MCX_PASS_MARCH_PERSISTENT  the z-march as one cooperative launch per run
+ *                    of sweeps, its passes separated by grid barriers (blocks
+ *                    of 128 or 256 threads; one wave of units).
  * No counterpart in the reference. */
-typedef enum { MCX_PASS_MARCH = 0, MCX_PASS_DIRECT = 1, MCX_PASS_STAGED = 2, MCX_PASS_MARCH_TMA = 3 } mcx_pass_kind;
+typedef enum {
+  MCX_PASS_MARCH = 0,
+  MCX_PASS_DIRECT = 1,
+  MCX_PASS_STAGED = 2,
+  MCX_PASS_MARCH_TMA = 3,
+  MCX_PASS_MARCH_ASYNC = 4,
+  MCX_PASS_MARCH_PERSISTENT = 5
+} mcx_pass_kind;
 mcx_status mcx_set_pass(mcx_engine *eng, int kind);
 int mcx_get_pass(const mcx_engine *eng);
 /* The z-march pass's shape: CTA size (64, 128 or 256 threads, one site pair
@@ -322,6 +336,12 @@ mcx_status mcx_pass_timing(mcx_engine *eng, int n_sweeps, float *pass_ms, float 
  * duration in the production launch sequence, launch gaps included.  The
  * sweeps are real (state, RNG counter and step size advance). */
 mcx_status mcx_sweep_timing(mcx_engine *eng, int n_sweeps, float *ms);
+/* Test of the persistent z-march's bounded grid-barrier wait: one launch
+ * whose barriers cannot complete.  Every CTA gives up after its poll limit
+ * (about a second), sets the error flag and leaves; returns MCX_ERR_CUDA with
+ * the barrier message (MCX_ERR_INVALID when that pass kind is not selected).
+ * The engine's directors are left mid-sweep. */
+mcx_status mcx_debug_barrier_timeout(mcx_engine *eng);
 
 /* Host-only helpers (no GPU needed). */
 /* setGHRL (src/io.cpp:277-302): out = lambda, mu, nu, rho, sigma. */

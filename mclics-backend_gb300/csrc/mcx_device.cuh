@@ -75,9 +75,10 @@ struct RepState {
   float ang_var;
   unsigned long long sweep;  // sweeps done: the RNG counter
   unsigned long long meas;   // measured sweeps done: the ring-slot counter
-  unsigned int acc[kLanes];  // accepted moves of the sweep in progress, by lane
-  unsigned int done;         // CTAs of the running colour-1 pass that finished
-  unsigned int frozen;        // nonzero: the step size stays fixed (no adaptation)
+  // the sweep in progress: accepted moves (low 32 bits; a replica has fewer
+  // than 2^31 sites) and work units of its colour-1 pass finished (high 32)
+  unsigned long long cnt;
+  unsigned int frozen;  // nonzero: the step size stays fixed (no adaptation)
 };
 
 // Running sums (doubles), indexed by the MCX_ST_* layout of mcx.h.

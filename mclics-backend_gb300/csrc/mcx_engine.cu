@@ -73,6 +73,8 @@ struct mcx_engine {
   int march_nt = 128, march_k = 8;
   bool pdl = true;  // programmatic dependent launch of the z-march passes
   bool tmarch = false;  // the z-march with rows staged by bulk copies (unmasked lattices)
+  bool amarch = false;  // the z-march with a per-thread cp.async prefetch (unmasked LL / GHRL)
+  bool pmarch = false;  // the z-march as one cooperative launch per run of sweeps (grid barriers)
   // learned-proposal z-march: its own units (128 pairs x kLearnPlanes planes)
   std::vector<int4> lunits;
   int4 *d_lunits = nullptr;
@@ -95,6 +97,7 @@ struct mcx_engine {
 static void drop_graphs(mcx_engine *e);
 static PassArgs pass_args(mcx_engine *e);
 static bool use_tmarch(mcx_engine *e, bool on);
+static mcx_status apply_march_shape(mcx_engine *e, int nt, int k);
 
 static mcx_status fail(mcx_engine *e, mcx_status st, const char *fmt, ...) {
   char buf[512];
@@ -248,12 +251,16 @@ static void plan_march(mcx_engine *e) {
   e->units.clear();
   const int nt = e->march_nt;
   double avg = 0.0;  // balanced: planes per unit
-  if (e->march_k <= 0) {
+  const int march_k = e->pmarch ? 0 : e->march_k;
+  if (march_k <= 0) {
     int dev = 0, nsm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    const long long slots = (long long)std::max(1, nsm) * std::max(1, march_blocks_per_sm(e->var, MODE_SWEEP, nt)) *
-                            std::max(1, -e->march_k);
+    const int per_sm = e->pmarch   ? pmarch_blocks_per_sm(e->var, nt)
+                       : e->amarch ? amarch_blocks_per_sm(e->var, nt)
+                                   : march_blocks_per_sm(e->var, MODE_SWEEP, nt);
+    // the persistent form needs every unit resident at once: one wave
+    const long long slots = (long long)std::max(1, nsm) * std::max(1, per_sm) * (e->pmarch ? 1 : std::max(1, -e->march_k));
     long long work = 0;
     for (const RepDev &R : e->rep) work += (long long)((R.hp * R.ny + nt - 1) / nt) * R.nz;
     avg = std::max(1.0, (double)work / (double)slots);
@@ -262,8 +269,8 @@ static void plan_march(mcx_engine *e) {
     RepDev &R = e->rep[r];
     const int npp = R.hp * R.ny;
     R.mcta = 0;
-    if (e->march_k > 0) {
-      const int K = std::min(e->march_k, R.nz);
+    if (march_k > 0) {
+      const int K = std::min(march_k, R.nz);
       for (int k0 = 0; k0 < R.nz; k0 += K)
         for (int p0 = 0; p0 < npp; p0 += nt) {
           e->units.push_back(make_int4(r, p0, k0, std::min(K, R.nz - k0)));
@@ -432,8 +439,8 @@ extern "C" mcx_status mcx_create(int n, const mcx_replica_desc *descs, mcx_engin
   CKC(cudaMalloc(&e->d_stats, sizeof(double) * kStats * n));
   CKC(cudaMemsetAsync(e->d_stats, 0, sizeof(double) * kStats * n, e->stream));
   CKC(cudaMalloc(&e->d_mout, sizeof(double) * 16 * n));
-  CKC(cudaMalloc(&e->d_err, sizeof(unsigned)));
-  CKC(cudaMemsetAsync(e->d_err, 0, sizeof(unsigned), e->stream));
+  CKC(cudaMalloc(&e->d_err, 2 * sizeof(unsigned)));  // the error flag, then the grid-barrier counter
+  CKC(cudaMemsetAsync(e->d_err, 0, 2 * sizeof(unsigned), e->stream));
   {
     int dev = 0, nsm = 0;
     CKC(cudaGetDevice(&dev));
@@ -691,6 +698,7 @@ static void launch_sweep_pass(mcx_engine *e, PassArgs &pa, int colour, bool meas
     }
   } else if (e->staged) launch_tpass(e->var, mode, pa, e->grid[measure ? 1 : 0], e->stream);
   else if (e->march && e->tmarch) launch_tmarch(e->var, mode, pa, e->march_nt, e->pdl, e->stream);
+  else if (e->march && e->amarch) launch_amarch(e->var, mode, pa, e->march_nt, e->pdl, e->stream);
   else if (e->march) launch_march(e->var, mode, pa, e->march_nt, e->pdl, e->stream);
   else launch_pass(e->var, mode, pa, e->pgrid[mode], e->stream);
 }
@@ -727,7 +735,34 @@ static mcx_status flush(mcx_engine *e) {
   return MCX_OK;
 }
 
+// Sweeps per cooperative launch of the persistent z-march (keeps its barrier
+// counter, 2 x sweeps x CTAs, far from 32-bit overflow).
+constexpr int kPersistentSweeps = 4096;
+
+// The persistent form's units must all be resident at once (a cooperative
+// launch of more CTAs than the GPU holds fails).
+static bool pmarch_fits(const mcx_engine *e) {
+  int dev = 0, nsm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  return (long long)e->units.size() <= (long long)nsm * pmarch_blocks_per_sm(e->var, e->march_nt);
+}
+
+static bool persistent(const mcx_engine *e) {
+  return e->pmarch && e->march && !e->staged && e->proposal == MCX_PROPOSAL_PLAIN;
+}
+
 static mcx_status run_sweeps(mcx_engine *e, int n, int m) {
+  if (persistent(e) && pmarch_fits(e)) {  // otherwise the register march below (bit-identical)
+    PassArgs pa = pass_args(e);
+    for (int done = 0; done < n;) {
+      const int k = std::min(n - done, kPersistentSweeps);
+      CK(e, launch_pmarch(e->var, m ? MODE_SWEEP_MEASURE : MODE_SWEEP, pa, e->march_nt, k, e->d_err + 1, e->stream));
+      e->launches += 1;
+      done += k;
+    }
+    return MCX_OK;
+  }
   if (n >= kChunk && !e->graph[m]) {
     if (mcx_status st = build_graph(e, m)) return st;
   }
@@ -766,6 +801,8 @@ static mcx_status check_err_flag(mcx_engine *e) {
   CK(e, cudaMemcpy(&f, e->d_err, sizeof f, cudaMemcpyDeviceToHost));
   if (f) {
     CK(e, cudaMemset(e->d_err, 0, sizeof f));
+    if (f & 2u)
+      return fail(e, MCX_ERR_CUDA, "persistent z-march: a grid barrier was not reached in time; results are invalid");
     return fail(e, MCX_ERR_CUDA, "staged pass: a shared-memory tile copy did not complete in time; results are invalid");
   }
   return MCX_OK;
@@ -779,26 +816,42 @@ extern "C" mcx_status mcx_sync(mcx_engine *e) {
 
 extern "C" mcx_status mcx_set_pass(mcx_engine *e, int kind) {
   if (!e) return fail(nullptr, MCX_ERR_INVALID, "null engine");
-  if (kind < MCX_PASS_MARCH || kind > MCX_PASS_MARCH_TMA) return fail(e, MCX_ERR_INVALID, "unknown pass kernel %d", kind);
+  if (kind < MCX_PASS_MARCH || kind > MCX_PASS_MARCH_PERSISTENT)
+    return fail(e, MCX_ERR_INVALID, "unknown pass kernel %d", kind);
   if (kind == MCX_PASS_STAGED && !e->can_stage)
     return fail(e, MCX_ERR_UNSUPPORTED, "a replica's rows do not fit the staged pass's shared memory");
   CK(e, cudaStreamSynchronize(e->stream));
   if (kind == MCX_PASS_MARCH_TMA && !use_tmarch(e, true))
     return fail(e, MCX_ERR_UNSUPPORTED, "the TMA-staged z-march needs an unmasked batch whose rows fit in shared memory");
+  if (kind == MCX_PASS_MARCH_ASYNC && !amarch_prepare(e->var, e->march_nt))
+    return fail(e, MCX_ERR_UNSUPPORTED, "the prefetching z-march needs an unmasked LL or GHRL batch");
+  if (kind == MCX_PASS_MARCH_PERSISTENT && !pmarch_block_ok(e->march_nt))
+    return fail(e, MCX_ERR_UNSUPPORTED, "the persistent z-march runs blocks of 128 or 256 threads");
   if (kind != MCX_PASS_MARCH_TMA) e->tmarch = false;
+  e->amarch = kind == MCX_PASS_MARCH_ASYNC;
+  e->pmarch = kind == MCX_PASS_MARCH_PERSISTENT;
   e->staged = kind == MCX_PASS_STAGED;
-  e->march = kind == MCX_PASS_MARCH || kind == MCX_PASS_MARCH_TMA;
-  for (int m = 0; m < 2; m++)
-    if (e->graph[m]) {
-      cudaGraphExecDestroy(e->graph[m]);
-      e->graph[m] = nullptr;
+  e->march = kind == MCX_PASS_MARCH || kind == MCX_PASS_MARCH_TMA || kind == MCX_PASS_MARCH_ASYNC ||
+             kind == MCX_PASS_MARCH_PERSISTENT;
+  if (e->march) {
+    if (mcx_status st = apply_march_shape(e, e->march_nt, e->march_k)) return st;  // chunks follow the form's residency
+    if (e->pmarch && !pmarch_fits(e)) {
+      e->pmarch = false;
+      apply_march_shape(e, e->march_nt, e->march_k);
+      return fail(e, MCX_ERR_UNSUPPORTED, "the persistent z-march needs every work unit resident at once; this batch has more column blocks than the GPU holds CTAs");
     }
+    return MCX_OK;
+  }
+  drop_graphs(e);
   return MCX_OK;
 }
 
 extern "C" int mcx_get_pass(const mcx_engine *e) {
   if (!e) return -1;
-  return e->staged ? MCX_PASS_STAGED : (e->march ? (e->tmarch ? MCX_PASS_MARCH_TMA : MCX_PASS_MARCH) : MCX_PASS_DIRECT);
+  if (e->staged) return MCX_PASS_STAGED;
+  if (!e->march) return MCX_PASS_DIRECT;
+  if (e->pmarch) return MCX_PASS_MARCH_PERSISTENT;
+  return e->tmarch ? MCX_PASS_MARCH_TMA : (e->amarch ? MCX_PASS_MARCH_ASYNC : MCX_PASS_MARCH);
 }
 
 extern "C" mcx_status mcx_set_staged(mcx_engine *e, int on) {
@@ -867,6 +920,7 @@ static mcx_status apply_march_shape(mcx_engine *e, int nt, int k) {
   e->march_nt = nt;
   e->march_k = k;
   const size_t before = e->units.size();
+  if (e->amarch) e->amarch = amarch_prepare(e->var, nt);  // before planning: its residency sets the waves
   plan_march(e);
   if (e->tmarch) use_tmarch(e, true);
   if (e->units.size() > before || !e->d_units) {
@@ -884,8 +938,16 @@ static mcx_status apply_march_shape(mcx_engine *e, int nt, int k) {
 extern "C" mcx_status mcx_set_march_shape(mcx_engine *e, int block, int planes) {
   if (!e) return fail(nullptr, MCX_ERR_INVALID, "null engine");
   if (!march_block_ok(block) || planes < -8) return fail(e, MCX_ERR_INVALID, "z-march shape %d threads x %d planes", block, planes);
+  if (e->pmarch && !pmarch_block_ok(block))
+    return fail(e, MCX_ERR_UNSUPPORTED, "the persistent z-march runs blocks of 128 or 256 threads");
   CK(e, cudaStreamSynchronize(e->stream));
   return apply_march_shape(e, block, planes);
+}
+
+static void launch_march_form(mcx_engine *e, int form, const PassArgs &pa, int nt) {
+  if (form == 1) launch_tmarch(e->var, MODE_SWEEP, pa, nt, e->pdl, e->stream);
+  else if (form == 2) launch_amarch(e->var, MODE_SWEEP, pa, nt, e->pdl, e->stream);
+  else launch_march(e->var, MODE_SWEEP, pa, nt, e->pdl, e->stream);
 }
 
 // Times the z-march pass for every candidate shape on a scratch copy of the
@@ -902,7 +964,7 @@ extern "C" mcx_status mcx_autotune(mcx_engine *e, int *block, int *planes, float
   const size_t ring_n = (size_t)e->nrep * (e->ring_cap + 1) * kLanes * kQ;
   cudaEvent_t t0, t1;
   mcx_status st = MCX_OK;
-  int best_nt = e->march_nt, best_k = e->march_k, best_tma = e->tmarch ? 1 : 0;
+  int best_nt = e->march_nt, best_k = e->march_k, best_form = e->pmarch ? 3 : (e->tmarch ? 1 : (e->amarch ? 2 : 0));
   float best = 1e30f;
 #define CKA(call)                                                                                    \
   do {                                                                                               \
@@ -923,33 +985,43 @@ extern "C" mcx_status mcx_autotune(mcx_engine *e, int *block, int *planes, float
   {
     const int nts[3] = {64, 128, 256};
     const int ks[10] = {1, 2, 4, 8, 16, 32, 0, -2, -3, -4};  // fixed depths, then balanced over 1..4 waves
-    for (int tma = 0; tma < 2; tma++)
+    // forms: 0 the register march, 1 rows staged by bulk copies, 2 the per-thread prefetch,
+    // 3 one cooperative launch per run of sweeps (one wave of units: a single shape per block size)
+    for (int form = 0; form < 4; form++)
     for (int a = 0; a < 3; a++)
       for (int ki = 0; ki < 10; ki++) {
         const int k = ks[ki];
         if (k > maxnz && k > 1) continue;
-        e->tmarch = tma != 0;
+        if (form == 3 && (k != 0 || !pmarch_block_ok(nts[a]) || pmarch_blocks_per_sm(e->var, nts[a]) == 0)) continue;
+        e->tmarch = form == 1;
+        e->amarch = form == 2;
+        e->pmarch = form == 3;
         if ((st = apply_march_shape(e, nts[a], k))) goto done;
-        if (tma && !e->tmarch) continue;  // the staged form cannot run this batch or shape
+        if ((form == 1 && !e->tmarch) || (form == 2 && !e->amarch) || (form == 3 && !pmarch_fits(e)))
+          continue;  // the form cannot run this batch
         PassArgs pa = pass_args(e);
         pa.dir = d_dir;
         pa.st = d_st;
         pa.stats = d_stats;
         pa.ring = d_ring;
         const int reps = 8;
-        for (int w = 0; w < 2; w++)
-          for (int c = 0; c < 2; c++) {
-            pa.colour = c;
-            if (tma) launch_tmarch(e->var, MODE_SWEEP, pa, nts[a], e->pdl, e->stream);
-            else launch_march(e->var, MODE_SWEEP, pa, nts[a], e->pdl, e->stream);
-          }
-        CKA(cudaEventRecord(t0, e->stream));
-        for (int q = 0; q < reps; q++)
-          for (int c = 0; c < 2; c++) {
-            pa.colour = c;
-            if (tma) launch_tmarch(e->var, MODE_SWEEP, pa, nts[a], e->pdl, e->stream);
-            else launch_march(e->var, MODE_SWEEP, pa, nts[a], e->pdl, e->stream);
-          }
+        if (form == 3) {
+          CKA(launch_pmarch(e->var, MODE_SWEEP, pa, nts[a], 2, e->d_err + 1, e->stream));
+          CKA(cudaEventRecord(t0, e->stream));
+          CKA(launch_pmarch(e->var, MODE_SWEEP, pa, nts[a], reps, e->d_err + 1, e->stream));
+        } else {
+          for (int w = 0; w < 2; w++)
+            for (int c = 0; c < 2; c++) {
+              pa.colour = c;
+              launch_march_form(e, form, pa, nts[a]);
+            }
+          CKA(cudaEventRecord(t0, e->stream));
+          for (int q = 0; q < reps; q++)
+            for (int c = 0; c < 2; c++) {
+              pa.colour = c;
+              launch_march_form(e, form, pa, nts[a]);
+            }
+        }
         CKA(cudaEventRecord(t1, e->stream));
         CKA(cudaGetLastError());
         CKA(cudaEventSynchronize(t1));
@@ -961,12 +1033,15 @@ extern "C" mcx_status mcx_autotune(mcx_engine *e, int *block, int *planes, float
           best = us;
           best_nt = nts[a];
           best_k = k;
-          best_tma = tma;
+          best_form = form;
         }
       }
   }
-  e->tmarch = best_tma != 0;
+  e->tmarch = best_form == 1;
+  e->amarch = best_form == 2;
+  e->pmarch = best_form == 3;
   st = apply_march_shape(e, best_nt, best_k);
+  if (st == MCX_OK) st = check_err_flag(e);
 done:
 #undef CKA
   cudaStreamSynchronize(e->stream);
@@ -1323,8 +1398,7 @@ extern "C" mcx_status mcx_load(mcx_engine *e, const char *path) {
     st[r].sweep = cs.sweep;
     st[r].meas = cs.meas;
     st[r].frozen = cs.frozen;
-    st[r].done = 0;
-    for (int l = 0; l < kLanes; l++) st[r].acc[l] = 0;
+    st[r].cnt = 0;
     e->desc[r].T = cs.T;
   }
   if (hdr[3] & 1u) {
@@ -1451,6 +1525,16 @@ extern "C" mcx_status mcx_combine_stats(mcx_engine *e, int n, const int *replica
   if (h[MCX_CB_T_SPREAD] > 1e-3)
     return fail(e, MCX_ERR_INVALID, "mcx_combine_stats: temperatures differ by %g (> 1e-3)", h[MCX_CB_T_SPREAD]);
   return MCX_OK;
+}
+
+extern "C" mcx_status mcx_debug_barrier_timeout(mcx_engine *e) {
+  if (!e) return fail(nullptr, MCX_ERR_INVALID, "null engine");
+  if (!persistent(e)) return fail(e, MCX_ERR_INVALID, "the persistent z-march is not selected");
+  PassArgs pa = pass_args(e);
+  CK(e, launch_pmarch(e->var, MODE_SWEEP, pa, e->march_nt, 1, e->d_err + 1, e->stream, 1u));
+  e->launches += 1;
+  CK(e, cudaStreamSynchronize(e->stream));
+  return check_err_flag(e);
 }
 
 extern "C" mcx_status mcx_measure(mcx_engine *e, int r, double *out) {

@@ -83,6 +83,20 @@ bool tmarch_prepare(const Variant &v, int nt, int smem_bytes);
 int tmarch_smem_bytes(const PassArgs &a);
 void launch_tmarch(const Variant &v, int mode, const PassArgs &a, int nt, bool pdl, cudaStream_t st);
 int march_blocks_per_sm(const Variant &v, int mode, int nt);
+// The z-march with a per-thread cp.async prefetch of the next plane
+// (mcx_amarch.cu; unmasked LL and GHRL): prepare once per block size.
+bool amarch_prepare(const Variant &v, int nt);
+int amarch_smem_bytes(int nt);
+int amarch_blocks_per_sm(const Variant &v, int nt);
+void launch_amarch(const Variant &v, int mode, const PassArgs &a, int nt, bool pdl, cudaStream_t st);
+// The z-march as one cooperative launch for nsweeps sweeps (mcx_pmarch.cu):
+// a.units must fit one wave (pmarch_blocks_per_sm per SM); bar is a counter
+// the launch zeroes first; extra > 0 makes every grid barrier unreachable
+// (a test of the bounded wait and its error flag).
+bool pmarch_block_ok(int nt);
+int pmarch_blocks_per_sm(const Variant &v, int nt);
+cudaError_t launch_pmarch(const Variant &v, int mode, const PassArgs &a, int nt, int nsweeps, unsigned *bar,
+                          cudaStream_t st, unsigned extra = 0);
 // The learned-proposal z-march (mcx_lmarch.cu): units of lmarch_block_threads()
 // pairs; lmarch_prepare sets its shared memory and checks residency.
 int lmarch_block_threads();

@@ -98,4 +98,124 @@ __device__ __forceinline__ void march_init(const PassArgs &a, const RepDev &R, i
     m.row = j + ny * kb;
 }
 
+// Resident CTAs per SM the compiler is asked for (measured best): the
+// unmasked Lebwohl-Lasher pass at about 96-113 registers per thread; the GHRL
+// and masked variants at 128 (they spill a little there, and still run 1.5x
+// faster than unconstrained at 160-206 registers, from the doubled occupancy).
+#ifndef MCX_MARCH_LL128_BLOCKS
+#define MCX_MARCH_LL128_BLOCKS 6
+#endif
+#ifndef MCX_MARCH_LL256_BLOCKS
+#define MCX_MARCH_LL256_BLOCKS 2
+#endif
+#ifndef MCX_MARCH_MASK_REGS
+#define MCX_MARCH_MASK_REGS 128
+#endif
+template <int POT, bool MASK, int NT>
+constexpr int march_min_blocks() {
+  return POT == POT_LL && !MASK ? (NT == 64 ? 9 : (NT == 128 ? MCX_MARCH_LL128_BLOCKS : MCX_MARCH_LL256_BLOCKS))
+                                : (MCX_MARCH_MASK_REGS > 0 ? 65536 / (NT * MCX_MARCH_MASK_REGS) : 1);
+}
+
+// The update of one same-colour pair from its loaded neighbourhood (shared by
+// the z-march and its staged and prefetching forms): own directors (ax, ay,
+// az) in and out; o0 the opposite pair of the same row, yp / ym those of rows
+// y+1 / y-1, op / om those of the planes above / below (zp / zm: those bonds
+// exist), exv the extra x neighbour; s the parity of the own sites in this
+// row; rw the pair's Philox draw (pair_draw below).
+template <int POT, bool MASK, bool FIELD, int MODE, bool PER>
+__device__ __forceinline__ void update_pair_draw(const PassArgs &a, const RepDev &R, int c, int s, bool hasB_,
+                                                 float ee0, float ee1, float eyp, float eym, const OPair &o0,
+                                                 const OPair &yp, const OPair &ym, const OPair &op, const OPair &om,
+                                                 const float exv[3], uint16_t pself, uint8_t pex, bool zp, bool zm,
+                                                 const uint4 rw, long long ns_at, float ang, float invT, float2 &ax,
+                                                 float2 &ay, float2 &az, unsigned &acc, float qs[kQ]) {
+  float uA[3], uB[3];
+  pair_uniforms(rw, uA, uB);
+  auto wt = [&](float ee, uint8_t pp) { return MASK ? (ee != 0.f && pp != 0 ? 1.f : 0.f) : ee; };
+  // PER: every bond exists (all axes periodic, pairs always complete)
+  const float exe = PER ? 1.f : (s ? ee1 : ee0);
+  const float erz[4] = {PER ? 1.f : eyp, PER ? 1.f : eym, PER || zp ? 1.f : 0.f, PER || zm ? 1.f : 0.f};
+  const bool hasB = PER || hasB_;
+  const OPair *rows4[4] = {&yp, &ym, &op, &om};
+  const uint8_t lo = (uint8_t)(o0.pt & 0xFF), hi = (uint8_t)(o0.pt >> 8);
+  const int P = R.plane;
+  float nb[6][3], w[6], e[6];
+  {  // site A
+    if (s == 0) {
+      nb[0][0] = o0.v[0].x; nb[0][1] = o0.v[1].x; nb[0][2] = o0.v[2].x; e[0] = 1.f; w[0] = wt(1.f, lo);
+      nb[1][0] = exv[0]; nb[1][1] = exv[1]; nb[1][2] = exv[2]; e[1] = exe; w[1] = wt(exe, pex);
+    } else {
+      if (hasB) {
+        nb[0][0] = o0.v[0].y; nb[0][1] = o0.v[1].y; nb[0][2] = o0.v[2].y; e[0] = 1.f; w[0] = wt(1.f, hi);
+      } else {
+        nb[0][0] = exv[0]; nb[0][1] = exv[1]; nb[0][2] = exv[2]; e[0] = exe; w[0] = wt(exe, pex);
+      }
+      nb[1][0] = o0.v[0].x; nb[1][1] = o0.v[1].x; nb[1][2] = o0.v[2].x; e[1] = 1.f; w[1] = wt(1.f, lo);
+    }
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      const OPair &o = *rows4[q];
+      nb[2 + q][0] = o.v[0].x; nb[2 + q][1] = o.v[1].x; nb[2 + q][2] = o.v[2].x;
+      e[2 + q] = erz[q];
+      w[2 + q] = wt(erz[q], MASK ? (uint8_t)(o.pt & 0xFF) : 1);
+    }
+    const int ps = MASK ? (pself & 0xFF) : 1;
+    float sx = 0.f, sy = 0.f, sz = 0.f;
+    if (MASK && ps > 1) {
+      const float *nsb = a.ns + R.ns_off + (long long)(c * 3) * P + ns_at;
+      sx = __ldg(nsb);
+      sy = __ldg(nsb + P);
+      sz = __ldg(nsb + 2 * P);
+    }
+    acc += site_update<POT, MASK, FIELD, MODE>(R, a, c, ax.x, ay.x, az.x, nb, w, e, ps, sx, sy, sz, uA, ang, invT,
+                                               0u, qs);
+  }
+  if (hasB) {  // site B
+    if (s == 0) {
+      nb[0][0] = o0.v[0].y; nb[0][1] = o0.v[1].y; nb[0][2] = o0.v[2].y; e[0] = 1.f; w[0] = wt(1.f, hi);
+      nb[1][0] = o0.v[0].x; nb[1][1] = o0.v[1].x; nb[1][2] = o0.v[2].x; e[1] = 1.f; w[1] = wt(1.f, lo);
+    } else {
+      nb[0][0] = exv[0]; nb[0][1] = exv[1]; nb[0][2] = exv[2]; e[0] = exe; w[0] = wt(exe, pex);
+      nb[1][0] = o0.v[0].y; nb[1][1] = o0.v[1].y; nb[1][2] = o0.v[2].y; e[1] = 1.f; w[1] = wt(1.f, hi);
+    }
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      const OPair &o = *rows4[q];
+      nb[2 + q][0] = o.v[0].y; nb[2 + q][1] = o.v[1].y; nb[2 + q][2] = o.v[2].y;
+      e[2 + q] = erz[q];
+      w[2 + q] = wt(erz[q], MASK ? (uint8_t)(o.pt >> 8) : 1);
+    }
+    const int ps = MASK ? (pself >> 8) : 1;
+    float sx = 0.f, sy = 0.f, sz = 0.f;
+    if (MASK && ps > 1) {
+      const float *nsb = a.ns + R.ns_off + (long long)(c * 3) * P + ns_at + 1;
+      sx = __ldg(nsb);
+      sy = __ldg(nsb + P);
+      sz = __ldg(nsb + 2 * P);
+    }
+    acc += site_update<POT, MASK, FIELD, MODE>(R, a, c, ax.y, ay.y, az.y, nb, w, e, ps, sx, sy, sz, uB, ang, invT,
+                                               0u, qs);
+  }
+}
+
+// The pair's Philox draw (counter: pair index, sweep, colour; key: seed,
+// stream), and update_pair_draw with it.
+__device__ __forceinline__ uint4 pair_draw(uint32_t pid, int c, unsigned long long sw, uint32_t seed, uint32_t stream) {
+  return philox4x32_10(make_uint4(pid, (uint32_t)sw, (uint32_t)(sw >> 32), TAG_PLAIN | (uint32_t)c), seed, stream);
+}
+
+template <int POT, bool MASK, bool FIELD, int MODE, bool PER>
+__device__ __forceinline__ void update_pair(const PassArgs &a, const RepDev &R, int c, int s, bool hasB_, float ee0,
+                                            float ee1, float eyp, float eym, const OPair &o0, const OPair &yp,
+                                            const OPair &ym, const OPair &op, const OPair &om, const float exv[3],
+                                            uint16_t pself, uint8_t pex, bool zp, bool zm, uint32_t pid,
+                                            long long ns_at, uint32_t seed, uint32_t stream, unsigned long long sw,
+                                            float ang, float invT, float2 &ax, float2 &ay, float2 &az, unsigned &acc,
+                                            float qs[kQ]) {
+  update_pair_draw<POT, MASK, FIELD, MODE, PER>(a, R, c, s, hasB_, ee0, ee1, eyp, eym, o0, yp, ym, op, om, exv, pself,
+                                                pex, zp, zm, pair_draw(pid, c, sw, seed, stream), ns_at, ang, invT, ax,
+                                                ay, az, acc, qs);
+}
+
 }  // namespace mcx

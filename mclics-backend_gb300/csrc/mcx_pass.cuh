@@ -200,17 +200,35 @@ __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)_
 // the replica's `total`, and lets the CTA that finishes the replica's last
 // unit of a colour-1 sweep pass apply the step-size rule and advance the sweep
 // counters.  Sums stay FP32 inside the CTA; one FP64 atomic per quantity.
+// Acceptances and finished units share one 64-bit counter, so a colour-0 CTA
+// leaves with a fire-and-forget atomic and a colour-1 CTA learns whether it
+// is the last (and the sweep's acceptance total) from a single atomic, with
+// no fences: the measurement ring is read by later kernels only.
+// colour: the pass's colour when the kernel runs several passes (a.colour
+// otherwise).  Replica state and running sums are read past L1 (__ldcg): a
+// kernel that runs several passes reads what other CTAs wrote in this launch.
 template <int NT, int MODE>
 __device__ __forceinline__ void flush_replica(const PassArgs &a, int r, int units, unsigned total, unsigned acc,
-                                              float qs[kQ], bool mask) {
+                                              float qs[kQ], bool mask, int colour = -1) {
   constexpr bool MEAS = MODE == MODE_SWEEP_MEASURE || MODE == MODE_MEASURE_ONLY;
   constexpr bool COUNT = MODE == MODE_SWEEP || MODE == MODE_SWEEP_MEASURE;
   __shared__ unsigned s_acc[NT / 32];
   __shared__ float s_q[NT / 32][kQ];
-  __shared__ unsigned s_last;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const RepDev &R = a.reps[r];
   RepState *S = a.st + r;
+  // what the step-size rule needs, loaded before the reductions so that the
+  // load latency overlaps them (only the last CTA of the sweep, which
+  // changes these, uses them, and it reads them before its own update)
+  float av0 = 0.f;
+  unsigned long long sweep0 = 0, meas0 = 0;
+  unsigned frozen0 = 0;
+  if (COUNT && threadIdx.x == 0) {
+    av0 = __ldcg(&S->ang_var);
+    sweep0 = __ldcg(&S->sweep);
+    meas0 = __ldcg(&S->meas);
+    frozen0 = __ldcg(&S->frozen);
+  }
   if (COUNT) {
     const unsigned wa = __reduce_add_sync(0xffffffffu, acc);
     if (lane == 0) s_acc[wid] = wa;
@@ -225,54 +243,51 @@ __device__ __forceinline__ void flush_replica(const PassArgs &a, int r, int unit
     }
   }
   __syncthreads();
-  const int lane_slot = blockIdx.x % kLanes;
-  if (COUNT && threadIdx.x == 0) {
-    unsigned tot = 0;
-#pragma unroll
-    for (int w2 = 0; w2 < NT / 32; w2++) tot += s_acc[w2];
-    if (tot) atomicAdd(&S->acc[lane_slot], tot);
-    __threadfence();
-  }
   if (MEAS && threadIdx.x < kQ) {
+    const int lane_slot = blockIdx.x % kLanes;
     const int q = (!mask && threadIdx.x == 1) ? 0 : threadIdx.x;
     float v = 0.f;
 #pragma unroll
     for (int w2 = 0; w2 < NT / 32; w2++) v += s_q[w2][q];
     const unsigned long long slot = MODE == MODE_MEASURE_ONLY ? (unsigned long long)a.ring_cap
-                                                              : S->meas % (unsigned long long)a.ring_cap;
+                                                              : __ldcg(&S->meas) % (unsigned long long)a.ring_cap;
     double *ring = a.ring + (((size_t)r * (a.ring_cap + 1) + slot) * kLanes + lane_slot) * kQ;
     atomicAdd(ring + threadIdx.x, (double)v);
-    __threadfence();
   }
-  if (COUNT && a.colour == 1) {
-    __syncthreads();
-    if (threadIdx.x == 0) s_last = atomicAdd(&S->done, (unsigned)units) + (unsigned)units == total;
-    __syncthreads();
-    if (s_last && threadIdx.x == 0) {
-      __threadfence();
-      unsigned tot = 0;
+  __syncwarp();  // warp 0's reads of the ring slot come before its thread 0 can end the sweep
+  if (COUNT && threadIdx.x == 0) {
+    unsigned tot = 0;
 #pragma unroll
-      for (int l = 0; l < kLanes; l++) tot += atomicExch(&S->acc[l], 0u);
-      // src/evolve.cpp:169-178 with the reference's float/double rounding
-      float av = S->ang_var;
-      const double ratio = 1.0 * (double)tot / (double)R.valid;
-      if (S->frozen) {
-      } else if (ratio < 0.5) {
-        av = (float)((double)av * 0.99);
-        if ((double)av < 0.01) av = (float)0.01;
-      } else if (ratio > 0.5) {
-        av = (float)((double)av / 0.99);
-        if ((double)av > 1.0) av = (float)((double)av - 0.5);
+    for (int w2 = 0; w2 < NT / 32; w2++) tot += s_acc[w2];
+    if ((colour < 0 ? a.colour : colour) != 1) {
+      if (tot) atomicAdd(&S->cnt, (unsigned long long)tot);
+    } else {
+      const unsigned long long add = ((unsigned long long)(unsigned)units << 32) | tot;
+      const unsigned long long old = atomicAdd(&S->cnt, add);
+      if ((unsigned)(old >> 32) + (unsigned)units == total) {  // the replica's last unit of the sweep
+        const unsigned sweep_acc = (unsigned)old + tot;
+        S->cnt = 0ull;
+        // src/evolve.cpp:169-178 with the reference's float/double rounding
+        float av = av0;
+        const double ratio = 1.0 * (double)sweep_acc / (double)R.valid;
+        if (frozen0) {
+        } else if (ratio < 0.5) {
+          av = (float)((double)av * 0.99);
+          if ((double)av < 0.01) av = (float)0.01;
+        } else if (ratio > 0.5) {
+          av = (float)((double)av / 0.99);
+          if ((double)av > 1.0) av = (float)((double)av - 0.5);
+        }
+        S->ang_var = av;
+        const unsigned long long sweep = sweep0 + 1;
+        S->sweep = sweep;
+        if (MODE == MODE_SWEEP_MEASURE) S->meas = meas0 + 1;
+        double *st = a.stats + (size_t)r * kStats;
+        atomicAdd(st + 7, (double)sweep_acc);
+        atomicAdd(st + 8, 1.0);
+        st[11] = (double)av;
+        st[12] = (double)sweep;
       }
-      S->ang_var = av;
-      S->sweep += 1;
-      if (MODE == MODE_SWEEP_MEASURE) S->meas += 1;
-      S->done = 0;
-      double *st = a.stats + (size_t)r * kStats;
-      st[7] += (double)tot;
-      st[8] += 1.0;
-      st[11] = (double)av;
-      st[12] = (double)S->sweep;
     }
   }
   __syncthreads();

@@ -30,7 +30,7 @@ BOUNDS = {"free": 0, "periodic": 1}
 ANCHORINGS = {"homeotropic": 0, "fg": 1, "rp": 2, "strong": 3, "homeotropic_ghrl": 4, "fg_ghrl": 5, "rp_ghrl": 6,
               "strong_ghrl": 7}
 PROPOSALS = {"plain": 0, "vmf_mlp": 1}
-PASSES = {"march": 0, "direct": 1, "staged": 2, "march_tma": 3}
+PASSES = {"march": 0, "direct": 1, "staged": 2, "march_tma": 3, "march_async": 4, "march_persistent": 5}
 MLP_PARAMS = 6792
 SAMPLE_FLOATS = 24
 AUG_FLIP, AUG_ROTATE = 1, 2
@@ -155,6 +155,7 @@ def lib() -> C.CDLL:
         L.mcx_stream.restype = V
         L.mcx_pass_timing.argtypes = [V, I, C.POINTER(F), C.POINTER(F)]
         L.mcx_sweep_timing.argtypes = [V, I, C.POINTER(F)]
+        L.mcx_debug_barrier_timeout.argtypes = [V]
         L.mcx_local_order.argtypes = [V, I, V]
         L.mcx_polarization.argtypes = [V, I, C.POINTER(C.c_double)]
         L.mcx_save.argtypes = [V, C.c_char_p]
@@ -392,7 +393,7 @@ class Engine:
 
     @property
     def pass_kind(self) -> str:
-        return {0: "march", 1: "direct", 2: "staged", 3: "march_tma"}[int(self._L.mcx_get_pass(self._h))]
+        return {v: k for k, v in PASSES.items()}[int(self._L.mcx_get_pass(self._h))]
 
     @pass_kind.setter
     def pass_kind(self, kind: str):

@@ -247,13 +247,14 @@ def test_errors_are_status_codes():
 
 
 KERNELS = [("march", 128, 8), ("march", 64, 1), ("march", 256, 32), ("march", 128, 3), ("march", 128, 0),
-           ("march", 64, -3), ("march_tma", 128, 8), ("march_tma", 256, 0), ("march_tma", 64, 3), ("direct", 0, 0),
-           ("staged", 0, 0)]
+           ("march", 64, -3), ("march_tma", 128, 8), ("march_tma", 256, 0), ("march_tma", 64, 3),
+           ("march_async", 256, 0), ("march_async", 128, 5), ("march_async", 64, 1), ("march_async", 256, 32),
+           ("march_persistent", 256, 0), ("march_persistent", 128, 0), ("direct", 0, 0), ("staged", 0, 0)]
 
 
 def _run_kernel(descs, setup, kind, block, planes, sweeps=19):
     with mcx.Engine(descs) as eng:
-        if kind in ("staged", "march_tma"):
+        if kind in ("staged", "march_tma", "march_async"):
             try:
                 eng.pass_kind = kind  # not every batch fits these kernels
             except mcx.McxError:
@@ -314,8 +315,41 @@ def test_pass_kernels_agree_on_uneven_batch():
             eng.set_state(r, random_state(m, np.ones(m.n, np.int32), np.random.default_rng(r)))
 
     ref = _run_kernel(descs, setup, "direct", 0, 0, sweeps=21)
-    for kind, block, planes in KERNELS[:9]:
+    for kind, block, planes in KERNELS[:15]:
         _assert_same(ref, _run_kernel(descs, setup, kind, block, planes, sweeps=21))
+
+
+def test_persistent_march_runs_split_like_one_run():
+    """The persistent z-march gives the same chain whether its sweeps run in
+    one cooperative launch or several, and the same as the register z-march."""
+    m = O.Model(nx=24, ny=20, nz=18, potential="ll")
+    d = desc_from_model(m, T=0.9, seed=5, stream=4)
+    ni0 = random_state(m, np.ones(m.n, np.int32), np.random.default_rng(11))
+    outs = []
+    for kind, runs in (("march_persistent", [37]), ("march_persistent", [1, 5, 31]), ("march", [37])):
+        with mcx.Engine([d]) as eng:
+            eng.pass_kind = kind
+            eng.set_march_shape(128, 0)
+            eng.set_state(0, ni0)
+            for n in runs:
+                eng.sweep(n, measure=True)
+            outs.append((eng.get_state(0), eng.stats(0)))
+    _assert_same(outs[0:1], outs[1:2])
+    _assert_same(outs[0:1], outs[2:3])
+
+
+def test_persistent_barrier_wait_is_bounded():
+    """A launch whose grid barriers cannot complete: every CTA gives up after
+    its poll limit and the engine reports the error; the GPU stays usable."""
+    m = O.Model(nx=16, ny=16, nz=16, potential="ll")
+    with mcx.Engine([desc_from_model(m, T=1.0)]) as eng:
+        eng.pass_kind = "march_persistent"
+        eng.set_march_shape(256, 0)
+        st = mcx.lib().mcx_debug_barrier_timeout(eng._h)
+        assert st == 2  # MCX_ERR_CUDA
+        assert "grid barrier" in mcx.lib().mcx_last_error(eng._h).decode()
+        eng.sweep(3)  # the engine and the context still work
+        eng.sync()
 
 
 def test_autotune_keeps_state_and_results():
