@@ -65,7 +65,7 @@ __global__ void __launch_bounds__(NT, march_min_blocks<POT, false, NT>()) k_amar
     const bool zper = R.zb == BOUND_PERIODIC;
     const int kb = u.z, ke = u.z + u.w;
     const uint32_t seed = R.seed, stream = R.stream;
-    grid_dependency_wait();  // directors and state may be written by the previous pass until here
+    grid_dependency_wait(m);  // directors and state may be written by the previous pass until here
     const unsigned long long sw = S->sweep;
     const float ang = S->ang_var, invT = 1.0f / S->T;
     OPair om, o0;

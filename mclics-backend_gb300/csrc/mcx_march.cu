@@ -36,7 +36,7 @@ __device__ __forceinline__ void march_plane(const PassArgs &a, const RepDev &R, 
   float2 ay = *reinterpret_cast<const float2 *>(m.A1 + m.off);
   float2 az = *reinterpret_cast<const float2 *>(m.A2 + m.off);
   const int dx = m.s ? m.dx1 : m.dx0;
-  const float exv[3] = {__ldg(m.O0 + m.off + dx), __ldg(m.O1 + m.off + dx), __ldg(m.O2 + m.off + dx)};
+  const float exv[3] = {ldg1(m.O0 + m.off + dx), ldg1(m.O1 + m.off + dx), ldg1(m.O2 + m.off + dx)};
   OPair yp, ym;
   load_opair_at<MASK>(m, m.off + m.dyp, m.offp + m.dypp, true, yp);
   load_opair_at<MASK>(m, m.off + m.dym, m.offp + m.dymp, true, ym);
@@ -76,7 +76,7 @@ __global__ void __launch_bounds__(NT, march_min_blocks<POT, MASK, NT>()) k_march
     // everything above depends only on constants; the state and the
     // directors may still be written by the previous pass (programmatic
     // dependent launch lets this grid start while that one drains)
-    grid_dependency_wait();
+    grid_dependency_wait(m);
     const unsigned long long sw = S->sweep;
     const float ang = S->ang_var, invT = 1.0f / S->T;
     // the z pipeline: opposite pairs of this column at planes k-1, k, k+1
@@ -225,7 +225,7 @@ __global__ void __launch_bounds__(NT, march_min_blocks<POT, false, NT>()) k_tmar
   sl.sa = a.tm_a;
   const float *Ob = a.dir + R.dir_off + (long long)((c ^ 1) * 3) * R.plane;
   float *Ag = a.dir + R.dir_off + (long long)(c * 3) * R.plane;
-  const int kb = u.z, ke = u.z + u.w, L = u.w;
+  const int kb = u.z, L = u.w;
   if (threadIdx.x == 0) {
     mbar_init(&bars[0], 1);
     mbar_init(&bars[1], 1);

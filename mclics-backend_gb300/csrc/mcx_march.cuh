@@ -8,7 +8,15 @@
 
 namespace mcx {
 
-__device__ __forceinline__ float2 ldg2(const float *p) { return __ldg(reinterpret_cast<const float2 *>(p)); }
+// Opposite-colour director loads of the z-march passes: L2 loads
+// (ld.global.cg).  A pass starts under programmatic dependent launch while
+// the previous pass, which writes these directors, drains; after
+// griddepcontrol.wait, read-only-path loads (__ldg) were seen to return lines
+// that an SM's L1 still held from before the previous pass's writes (the
+// chain then differed from a launch-by-launch run), while L2 loads always
+// see them.
+__device__ __forceinline__ float2 ldg2(const float *p) { return __ldcg(reinterpret_cast<const float2 *>(p)); }
+__device__ __forceinline__ float ldg1(const float *p) { return __ldcg(p); }
 
 // Programmatic dependent launch: wait until the preceding grid on the stream
 // has completed and its memory is visible (returns at once when the launch
@@ -39,6 +47,17 @@ struct March {
   bool hasB;
   float ee0, ee1, eyp, eym;         // bond present: extra x (s = 0, 1), y+1, y-1
 };
+
+// griddepcontrol.wait for a march whose director pointers are in m.  The
+// pointers pass through the asm as operands, so every director address is
+// computed from values that exist only after the wait, and no load through
+// them can be scheduled above it, whatever its cache path.
+__device__ __forceinline__ void grid_dependency_wait(March &m) {
+  asm volatile("griddepcontrol.wait;"
+               : "+l"(m.A0), "+l"(m.A1), "+l"(m.A2), "+l"(m.O0), "+l"(m.O1), "+l"(m.O2)
+               :
+               : "memory");
+}
 
 template <bool MASK>
 __device__ __forceinline__ void load_opair_at(const March &m, int off, int offp, bool on, OPair &o) {

@@ -64,6 +64,8 @@ def run(L: int = 96, temps: Sequence[float] = (1.00, 1.10, 1.12, 1.15), per_T: i
         eng.sweep(equil)
         eng.sync()
         say(f"equilibrated {equil} sweeps in {time.perf_counter() - t0:.1f}s")
+        # the plain sampler runs with the pass shape the autotuner picks for this batch
+        out["plain_pass"] = list(eng.autotune()[:2]) + [eng.pass_kind]
         # training on plain-sampler equilibrium configurations
         eng.set_mlp(init_weights(seed))
         t0 = time.perf_counter()
