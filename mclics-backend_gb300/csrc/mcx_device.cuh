@@ -62,6 +62,10 @@ struct RepDev {
   long long ns_off;   // float offset of its [2][3][plane] normals
   float A, elecA, elecE, ex, ey, ez;
   float lam, mu, nu, rho, sigma;
+  // the GHRL bond regrouped for the pass (ghrl_bond_var): ga = 1.5 rho,
+  // gb = lambda - rho / 2, gc = 1.5 nu; gconst = -nu / 2 - mu / 9 the part
+  // every bond shares
+  float ga, gb, gc, gconst;
   float B1, C;  // Pear potential
   uint32_t seed, stream;
   int anch[kMaxSurf];
@@ -157,6 +161,25 @@ __device__ __forceinline__ float ghrl_bond(const RepDev &R, float ax, float ay, 
   const float cr = sign * cross_ref<AXIS>(ax, ay, az, bx, by, bz);
   const float sg = nij > 0.f ? 1.f : -1.f;
   return E1 * (R.rho * P2 + R.lam) + R.mu * (ai * aj * nij - (1.0f / 9.0f)) + R.nu * P2 + R.sigma * sg * cr;
+}
+
+// The GHRL bond without its constant part, as the pass evaluates it:
+// ghrl_bond = ghrl_bond_var + gconst.  Regrouped as
+// E1 (ga q + gb) + gc q + mu aj ai nij + sigma sgn(nij) cr, q = nij^2,
+// E1 = 1.5 ai^2 + (1.5 aj^2 - 1): the neighbour-only terms (1.5 aj^2 - 1,
+// mu aj) are shared by the old and the new director's evaluation, and the
+// constant drops out of every energy difference (measurements add
+// gconst per bond).
+template <int AXIS>
+__device__ __forceinline__ float ghrl_bond_var(const RepDev &R, float ax, float ay, float az, float bx, float by,
+                                               float bz, float sign) {
+  const float ai = AXIS == 0 ? ax : (AXIS == 1 ? ay : az);
+  const float aj = AXIS == 0 ? bx : (AXIS == 1 ? by : bz);
+  const float nij = ax * bx + ay * by + az * bz;
+  const float q = nij * nij;
+  const float E1 = 1.5f * ai * ai + (1.5f * aj * aj - 1.0f);
+  const float cr = sign * cross_ref<AXIS>(ax, ay, az, bx, by, bz);
+  return E1 * (R.ga * q + R.gb) + R.gc * q + (R.mu * aj) * (ai * nij) + R.sigma * (nij > 0.f ? cr : -cr);
 }
 
 // Anchoring energy of surface `sid` (src/anchoring_*.cpp, CPU semantics).

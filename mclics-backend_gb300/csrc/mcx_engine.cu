@@ -353,6 +353,10 @@ extern "C" mcx_status mcx_create(int n, const mcx_replica_desc *descs, mcx_engin
     R.nu = g[2];
     R.rho = g[3];
     R.sigma = g[4];
+    R.ga = 1.5f * R.rho;
+    R.gb = R.lam - 0.5f * R.rho;
+    R.gc = 1.5f * R.nu;
+    R.gconst = d.potential == MCX_POT_GHRL ? -0.5f * R.nu - R.mu / 9.0f : 0.0f;
     R.seed = d.seed;
     R.stream = d.stream;
     for (int s = 0; s < d.n_surfaces; s++) {

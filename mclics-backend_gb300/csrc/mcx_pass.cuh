@@ -45,7 +45,7 @@ __device__ __forceinline__ float bond(const RepDev &R, float ax, float ay, float
     const float splay = (1.f + 2.f * nij + nij * nij) * d;
     return -R.A * nij * nij - R.B1 * nij - (R.C * 0.25f) * splay;
   } else {
-    return ghrl_bond<(D >> 1)>(R, ax, ay, az, b[0], b[1], b[2], (D & 1) ? -1.f : 1.f);
+    return ghrl_bond_var<(D >> 1)>(R, ax, ay, az, b[0], b[1], b[2], (D & 1) ? -1.f : 1.f);
   }
 }
 
@@ -77,6 +77,14 @@ __device__ __forceinline__ float bond_sum(const RepDev &R, float ax, float ay, f
 template <int POT>
 __device__ __forceinline__ float bond_scale(const RepDev &R) {
   return POT == POT_LL ? -1.5f * R.A : 1.f;
+}
+
+// The part of a weighted bond sum that bond() leaves out (the GHRL bond's
+// constant per bond); measurements add it, energy differences do not need it.
+template <int POT>
+__device__ __forceinline__ float bond_const(const RepDev &R, const float w[6]) {
+  if (POT != POT_GHRL) return 0.f;
+  return R.gconst * (((w[0] + w[1]) + (w[2] + w[3])) + (w[4] + w[5]));
 }
 
 // Rotated proposal (src/evolve.cpp:136-152 / src/evolve.cu:143-163): rotate by
@@ -176,17 +184,17 @@ __device__ __forceinline__ unsigned site_update(const RepDev &R, const PassArgs 
       // each bond counts in the local energy of each active end; the
       // all-site energy also counts inactive sites' bonds to active ones
       if (pself != 0) {
-        const float ebs = bond_scale<POT>(R) * eb;
+        const float ebs = bond_scale<POT>(R) * eb + bond_const<POT>(R, w);
         qs[0] += 2.f * ebs;
         qs[1] += 2.f * ebs;
         if (MASK) {
           float wi[6];
 #pragma unroll
           for (int d = 0; d < 6; d++) wi[d] = e[d] - w[d];
-          qs[0] += bond_scale<POT>(R) * bond_sum<POT>(R, x, y, z, nb, wi);
+          qs[0] += bond_scale<POT>(R) * bond_sum<POT>(R, x, y, z, nb, wi) + bond_const<POT>(R, wi);
         }
       } else {
-        qs[0] += bond_scale<POT>(R) * bond_sum<POT>(R, x, y, z, nb, w);
+        qs[0] += bond_scale<POT>(R) * bond_sum<POT>(R, x, y, z, nb, w) + bond_const<POT>(R, w);
       }
     }
   }
@@ -570,17 +578,17 @@ __device__ __forceinline__ unsigned site_update_learned(const RepDev &R, const P
     }
     if (c == 1) {
       if (pself != 0) {
-        const float ebs = bond_scale<POT>(R) * eb;
+        const float ebs = bond_scale<POT>(R) * eb + bond_const<POT>(R, w);
         qs[0] += 2.f * ebs;
         qs[1] += 2.f * ebs;
         if (MASK) {
           float wi[6];
 #pragma unroll
           for (int d = 0; d < 6; d++) wi[d] = e[d] - w[d];
-          qs[0] += bond_scale<POT>(R) * bond_sum<POT>(R, x, y, z, nb, wi);
+          qs[0] += bond_scale<POT>(R) * bond_sum<POT>(R, x, y, z, nb, wi) + bond_const<POT>(R, wi);
         }
       } else {
-        qs[0] += bond_scale<POT>(R) * bond_sum<POT>(R, x, y, z, nb, w);
+        qs[0] += bond_scale<POT>(R) * bond_sum<POT>(R, x, y, z, nb, w) + bond_const<POT>(R, w);
       }
     }
   }
