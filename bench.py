@@ -388,10 +388,14 @@ def main():
     achieved = bytes_per_launch / (per_launch_ms * 1e-3) / 1e9
     peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(peaks_path):
-        peak = json.load(open(peaks_path))["hbm_gbs"]
+        pk = json.load(open(peaks_path))
+        peak, bf16_peak = pk["hbm_gbs"], pk.get("bf16_tflops_sustained", pk.get("bf16_tflops"))
         peak_src = "measured"
     else:
-        peak, peak_src = 6800.0, "fallback"
+        peak, bf16_peak, peak_src = 6800.0, 1700.0, "fallback"
+    from mcx.gain import MLP_FLOP_PER_UPDATE
+    flops_per_launch = MLP_FLOP_PER_UPDATE * SITES * R / 2  # one colour: half the sites
+    mlp_tflops = flops_per_launch / (per_launch_ms * 1e-3) / 1e12
     traffic = None
     tpath = os.path.join(ROOT, "profiles", f"sweep_pass_ll{NX}.md" if R == 1 else f"sweep_pass_ll{NX}x{R}.md")
     if os.path.exists(tpath):
@@ -454,9 +458,17 @@ def main():
                                          f"{max(1, -tuned[1])} wave(s) of resident CTAs ({how})")
                                    if args.proposal == "plain" else "learned-proposal z-march (k_lmarch, BF16 MLP)"),
                    "S_E_last_step": [rows[-1][0], rows[-1][1], rows[-1][2]] if rows else None},
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": traffic, "peak_source": peak_src, "kernel": FORMS[form][0] if args.proposal == "plain" else "k_lmarch<LL> (learned proposal)",
-                     "bytes_per_launch": bytes_per_launch, "launch_ms": per_launch_ms,
+        "roofline": ({"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                      "traffic": traffic, "peak_source": peak_src, "kernel": FORMS[form][0],
+                      "bytes_per_launch": bytes_per_launch}
+                     if args.proposal == "plain" else
+                     # the learned pass is bound by its BF16 MLP: 11.1 kFLOP per site-update against
+                     # the sustained dense BF16 rate (the pass runs for seconds back to back)
+                     {"bound": "tensor", "achieved": mlp_tflops, "peak": bf16_peak, "unit": "TFLOP/s",
+                      "frac": mlp_tflops / bf16_peak, "traffic": None, "peak_source": peak_src,
+                      "kernel": "k_lmarch<LL> (learned proposal, mma.sync BF16 MLP)",
+                      "flops_per_launch": flops_per_launch, "hbm_achieved_gbs": achieved}) | {
+                     "launch_ms": per_launch_ms,
                      "launch_ms_isolated": per_launch_isolated_ms,
                      "launch_ms_method": ("400 unmeasured sweeps in cooperative launches between two CUDA events "
                                           "on the engine stream / 800 passes" if form == "march_persistent" else
