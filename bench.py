@@ -289,6 +289,7 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl")
     import mcx
+    from mcx.shard import max_over_ranks
 
     temps = temperatures()
     descs = [mcx.replica(nx=NX, ny=NY, nz=NZ, potential="ll", A=1.0, T=temps[0], ang_var=0.5, seed=1 + rank * R + q,
@@ -358,10 +359,7 @@ def main():
         dist.barrier()
     launches = eng.kernel_launches - launches0
     total_ms = sum(a.elapsed_time(b) for a, b in ev)
-    if dist:
-        t = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(total_ms)  # the slowest rank's time (identity on one GPU)
     per_step_ms = total_ms / nsteps
     updates_per_step = (MCT + MCS) * SITES * R
     value = ws * updates_per_step * nsteps / (total_ms / 1e3)
@@ -430,10 +428,7 @@ def main():
                 if L.mcx_get_state(eng._h, q, pout):
                     raise RuntimeError(L.mcx_last_error(eng._h).decode())
         e2e_s = time.perf_counter() - t0
-        if dist:
-            t = torch.tensor([e2e_s], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            e2e_s = float(t.item())
+        e2e_s = max_over_ranks(e2e_s)
         e2e = {"value": ws * updates_per_step * nsteps / e2e_s, "unit": "site-updates/s",
                "h2d_bytes_per_step": 12 * SITES * R, "d2h_bytes_per_step": 12 * SITES * R + 16 * 8}
 
