@@ -178,8 +178,12 @@ __device__ __forceinline__ float ghrl_bond_var(const RepDev &R, float ax, float 
   const float nij = ax * bx + ay * by + az * bz;
   const float q = nij * nij;
   const float E1 = 1.5f * ai * ai + (1.5f * aj * aj - 1.0f);
-  const float cr = sign * cross_ref<AXIS>(ax, ay, az, bx, by, bz);
-  return E1 * (R.ga * q + R.gb) + R.gc * q + (R.mu * aj) * (ai * nij) + R.sigma * (nij > 0.f ? cr : -cr);
+  float v = E1 * (R.ga * q + R.gb) + R.gc * q + (R.mu * aj) * (ai * nij);
+  if (R.sigma != 0.f) {  // the chiral term (p0 != 0); the branch is uniform: a CTA serves one replica
+    const float cr = sign * cross_ref<AXIS>(ax, ay, az, bx, by, bz);
+    v += R.sigma * (nij > 0.f ? cr : -cr);
+  }
+  return v;
 }
 
 // Anchoring energy of surface `sid` (src/anchoring_*.cpp, CPU semantics).
