@@ -63,7 +63,7 @@ __global__ void __launch_bounds__(NT, march_min_blocks<POT, false, NT>()) k_amar
     March m;
     march_init<false>(a, R, c, p, u.z, m);
     const bool zper = R.zb == BOUND_PERIODIC;
-    const int kb = u.z, ke = u.z + u.w;
+    const int kb = u.z, ke = u.z + (u.w & kUnitPlanes);
     const uint32_t seed = R.seed, stream = R.stream;
     grid_dependency_wait(m);  // directors and state may be written by the previous pass until here
     const unsigned long long sw = S->sweep;

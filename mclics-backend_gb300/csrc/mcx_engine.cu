@@ -75,6 +75,8 @@ struct mcx_engine {
   bool tmarch = false;  // the z-march with rows staged by bulk copies (unmasked lattices)
   bool amarch = false;  // the z-march with a per-thread cp.async prefetch (unmasked LL / GHRL)
   bool pmarch = false;  // the z-march as one cooperative launch per run of sweeps (grid barriers)
+  // per replica of a masked batch: row j + ny * k holds an active site (empty: unknown)
+  std::vector<std::vector<uint8_t>> rowact;
   // learned-proposal z-march: its own units (128 pairs x kLearnPlanes planes)
   std::vector<int4> lunits;
   int4 *d_lunits = nullptr;
@@ -247,6 +249,36 @@ static void effective_bounds(mcx_replica_desc &d) {
 // the column blocks of all replicas are cut into chunks of near-equal depth
 // (sizes differ by at most one plane) so that the units fill max(1, -march_k)
 // waves, which keeps the last wave from running mostly idle.
+// A unit of a masked replica is dead when its rows and planes, and the rows
+// and planes next to them, hold no active site (kUnitDead).
+static bool unit_dead(const mcx_engine *e, const int4 &u) {
+  const std::vector<uint8_t> &act = e->rowact[u.x];
+  if (act.empty()) return false;
+  const RepDev &R = e->rep[u.x];
+  const int pend = std::min(u.y + e->march_nt, R.hp * R.ny);
+  const int j0 = u.y / R.hp, j1 = (pend - 1) / R.hp, nk = u.w & kUnitPlanes;
+  for (int k = u.z - 1; k <= u.z + nk; k++) {
+    int kk = k;
+    if (kk < 0 || kk >= R.nz) {
+      if (R.zb != BOUND_PERIODIC) continue;
+      kk = (kk + R.nz) % R.nz;
+    }
+    for (int j = j0 - 1; j <= j1 + 1; j++) {
+      int jj = j;
+      if (jj < 0 || jj >= R.ny) {
+        if (R.yb != BOUND_PERIODIC) continue;
+        jj = (jj + R.ny) % R.ny;
+      }
+      if (act[(size_t)jj + (size_t)R.ny * kk]) return false;
+    }
+  }
+  return true;
+}
+
+static void mark_dead_units(mcx_engine *e) {
+  for (int4 &u : e->units) u.w = (u.w & kUnitPlanes) | (unit_dead(e, u) ? kUnitDead : 0);
+}
+
 static void plan_march(mcx_engine *e) {
   e->units.clear();
   const int nt = e->march_nt;
@@ -288,6 +320,7 @@ static void plan_march(mcx_engine *e) {
       }
     }
   }
+  mark_dead_units(e);
 }
 
 extern "C" mcx_status mcx_create(int n, const mcx_replica_desc *descs, mcx_engine **out) {
@@ -312,6 +345,7 @@ extern "C" mcx_status mcx_create(int n, const mcx_replica_desc *descs, mcx_engin
   e->var.per = true;
   long long dir_total = 0, pt_total = 0;
   e->rep.resize(n);
+  e->rowact.resize(n);
   for (int r = 0; r < n; r++) {
     mcx_replica_desc &d = e->desc[r];
     effective_bounds(d);
@@ -605,6 +639,21 @@ extern "C" mcx_status mcx_set_mask(mcx_engine *e, int r, const int *pt, const fl
   CKL(e);
   R.valid = (int)v;
   CK(e, cudaMemcpyAsync(&e->d_rep[r].valid, &R.valid, sizeof(int), cudaMemcpyHostToDevice, e->stream));
+  // which rows hold an active site: z-march units far from every one skip their updates
+  std::vector<uint8_t> &act = e->rowact[r];
+  act.assign((size_t)R.ny * R.nz, 0);
+  for (long row = 0; row < (long)R.ny * R.nz; row++)
+    for (int i = 0; i < R.nx; i++)
+      if (pt[row * R.nx + i]) {
+        act[row] = 1;
+        break;
+      }
+  if (e->d_units && !e->units.empty()) {
+    mark_dead_units(e);
+    CK(e, cudaMemcpyAsync(e->d_units, e->units.data(), sizeof(int4) * e->units.size(), cudaMemcpyHostToDevice,
+                          e->stream));
+    drop_graphs(e);
+  }
   CK(e, cudaStreamSynchronize(e->stream));
   return MCX_OK;
 }

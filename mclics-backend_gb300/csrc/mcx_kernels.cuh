@@ -27,6 +27,15 @@ enum PassMode : int {
   MODE_TRACE = 3          // update one colour of one replica and record every site
 };
 
+// z-march work units are int4 (replica, first pair, first plane, planes |
+// flags).  kUnitDead marks a unit of a masked replica whose rows and planes,
+// and the rows and planes next to them, hold no active site: its sites never
+// move and have no bond to an active site, so its only work is the field
+// energy of its sites in measured sweeps (what the full update adds for an
+// inactive site).
+constexpr int kUnitDead = 1 << 30;
+constexpr int kUnitPlanes = kUnitDead - 1;
+
 struct PassArgs {
   const RepDev *reps;
   const int2 *map;  // work units of the direct pass: (replica, first same-colour pair)

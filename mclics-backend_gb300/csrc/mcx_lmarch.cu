@@ -53,7 +53,7 @@ __global__ void __launch_bounds__(kLPB, MCX_LMARCH_MIN_BLOCKS) k_lmarch(PassArgs
   march_init<MASK>(a, R, c, p, u.z, m);
   const int nz = R.nz, nx = R.nx;
   const bool zper = R.zb == BOUND_PERIODIC;
-  const int kb = u.z, ke = u.z + u.w;
+  const int kb = u.z, ke = u.z + (u.w & kUnitPlanes);
   unsigned acc = 0;
   float qs[kQ];
 #pragma unroll

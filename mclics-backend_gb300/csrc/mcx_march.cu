@@ -71,12 +71,15 @@ __global__ void __launch_bounds__(NT, march_min_blocks<POT, MASK, NT>()) k_march
     March m;
     march_init<MASK>(a, R, c, p, u.z, m);
     const bool zper = R.zb == BOUND_PERIODIC;
-    const int kb = u.z, ke = u.z + u.w;
+    const int kb = u.z, ke = u.z + (u.w & kUnitPlanes);
     const uint32_t seed = R.seed, stream = R.stream;
     // everything above depends only on constants; the state and the
     // directors may still be written by the previous pass (programmatic
     // dependent launch lets this grid start while that one drains)
     grid_dependency_wait(m);
+    if (MASK && (u.w & kUnitDead)) {
+      dead_unit<FIELD, MODE>(R, m, kb, ke, qs);
+    } else {
     const unsigned long long sw = S->sweep;
     const float ang = S->ang_var, invT = 1.0f / S->T;
     // the z pipeline: opposite pairs of this column at planes k-1, k, k+1
@@ -102,6 +105,7 @@ __global__ void __launch_bounds__(NT, march_min_blocks<POT, MASK, NT>()) k_march
       m.pid += m.dpid;
       m.row += R.ny;
       m.s ^= 1;
+    }
     }
   }
   grid_dependency_wait();    // threads without a pair reach here without having waited

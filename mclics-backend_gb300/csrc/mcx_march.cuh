@@ -59,6 +59,23 @@ __device__ __forceinline__ void grid_dependency_wait(March &m) {
                : "memory");
 }
 
+// A dead unit (kUnitDead) of a masked lattice: in measured sweeps with a
+// field, each own (inactive) site adds its field energy, in the order the
+// full update adds it; nothing else.
+template <bool FIELD, int MODE>
+__device__ __forceinline__ void dead_unit(const RepDev &R, March &m, int kb, int ke, float qs[kQ]) {
+  if (!(FIELD && MODE == MODE_SWEEP_MEASURE)) return;
+#pragma unroll 1
+  for (int k = kb; k < ke; k++) {
+    const float2 x = *reinterpret_cast<const float2 *>(m.A0 + m.off);
+    const float2 y = *reinterpret_cast<const float2 *>(m.A1 + m.off);
+    const float2 z = *reinterpret_cast<const float2 *>(m.A2 + m.off);
+    qs[0] += field_energy(R, x.x, y.x, z.x);
+    if (m.hasB) qs[0] += field_energy(R, x.y, y.y, z.y);
+    m.off += m.dz;
+  }
+}
+
 template <bool MASK>
 __device__ __forceinline__ void load_opair_at(const March &m, int off, int offp, bool on, OPair &o) {
   if (on) {

@@ -117,7 +117,8 @@ __global__ void __launch_bounds__(NT, march_min_blocks<POT, MASK, NT>())
   const bool has_pair = p < R.hp * R.ny;
   const int nz = R.nz;
   const bool zper = R.zb == BOUND_PERIODIC;
-  const int kb = u.z, ke = u.z + u.w;
+  const int kb = u.z, ke = u.z + (u.w & kUnitPlanes);
+  const bool dead = MASK && (u.w & kUnitDead);
   const uint32_t seed = R.seed, stream = R.stream;
   unsigned target = extra;  // extra > 0 only to test the bounded wait: no barrier completes
 #pragma unroll 1
@@ -127,7 +128,11 @@ __global__ void __launch_bounds__(NT, march_min_blocks<POT, MASK, NT>())
     float qs[kQ];
 #pragma unroll
     for (int q = 0; q < kQ; q++) qs[q] = 0.f;
-    if (has_pair) {
+    if (has_pair && dead) {
+      March m;
+      march_init<MASK>(a, R, c, p, kb, m);
+      dead_unit<FIELD, MODE>(R, m, kb, ke, qs);
+    } else if (has_pair) {
       March m;
       march_init<MASK>(a, R, c, p, kb, m);
       const unsigned long long sw = __ldcg(&S->sweep);
