@@ -293,8 +293,16 @@ static void plan_march(mcx_engine *e) {
                                    : march_blocks_per_sm(e->var, MODE_SWEEP, nt);
     // the persistent form needs every unit resident at once: one wave
     const long long slots = (long long)std::max(1, nsm) * std::max(1, per_sm) * (e->pmarch ? 1 : std::max(1, -e->march_k));
+    // work: column blocks x planes, without the dead ones (no active site in or next to them),
+    // which cost next to nothing; the persistent form counts every unit, all resident at once
     long long work = 0;
-    for (const RepDev &R : e->rep) work += (long long)((R.hp * R.ny + nt - 1) / nt) * R.nz;
+    for (int r = 0; r < e->nrep; r++) {
+      const RepDev &R = e->rep[r];
+      const int npp = R.hp * R.ny;
+      for (int p0 = 0; p0 < npp; p0 += nt)
+        for (int k = 0; k < R.nz; k++)
+          work += e->pmarch || !unit_dead(e, make_int4(r, p0, k, 1)) ? 1 : 0;
+    }
     avg = std::max(1.0, (double)work / (double)slots);
   }
   for (int r = 0; r < e->nrep; r++) {

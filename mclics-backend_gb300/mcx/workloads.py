@@ -125,6 +125,8 @@ def run_c5(replicas=64, sweeps=20, proposal="plain", side=96, radius=40.0, train
     with Engine(descs) as eng:
         for q in range(replicas):
             eng.init_random(q, 11 + q)
+        tuned = eng.autotune()
+        out["pass_kernel"] = f"{eng.pass_kind} {tuned[0]} x {tuned[1]} (autotuned)"
         eng.sweep(200)
         if proposal != "plain":
             eng.set_mlp(gain.init_weights(5))
