@@ -90,10 +90,12 @@ void pack_mlp_weights(const float *flat, uint8_t *out) {
   uint16_t *w3t = reinterpret_cast<uint16_t *>(out + kMlpW3);
   for (int n = 0; n < kMlpH; n++)
     for (int k = 0; k < kMlpIn; k++) w1t[n * kW1s + k] = to_bf16(W1[k * kMlpH + n]);
+  // layers 2 and 3 take twice the GELU (gelu_bf16x2): their weights at half
+  // scale, exactly (bf16(w / 2) = bf16(w) / 2 for weights above 1e-38)
   for (int n = 0; n < kMlpH; n++)
-    for (int k = 0; k < kMlpH; k++) w2t[n * kW2s + k] = to_bf16(W2[k * kMlpH + n]);
+    for (int k = 0; k < kMlpH; k++) w2t[n * kW2s + k] = to_bf16(0.5f * W2[k * kMlpH + n]);
   for (int n = 0; n < kMlpOut; n++)
-    for (int k = 0; k < kMlpH; k++) w3t[n * kW3s + k] = to_bf16(W3[k * kMlpOut + n]);
+    for (int k = 0; k < kMlpH; k++) w3t[n * kW3s + k] = to_bf16(0.5f * W3[k * kMlpOut + n]);
   memcpy(out + kMlpB1, b1, kMlpH * 4);
   memcpy(out + kMlpB2, b2, kMlpH * 4);
   memcpy(out + kMlpB3, b3, kMlpOut * 4);

@@ -10,8 +10,8 @@
 //
 // Shared-memory weight layout (also the device buffer's layout, bytes):
 //   W1t [64][40] bf16   W1 transposed: row n holds k = 0..31 (19..31 zero), 8 pad
-//   W2t [64][72] bf16   W2 transposed, 8 pad
-//   W3t [ 8][72] bf16   W3 transposed (n = 0..7, outputs 4..7 zero)
+//   W2t [64][72] bf16   W2 transposed and halved (gelu_bf16x2 returns twice the GELU), 8 pad
+//   W3t [ 8][72] bf16   W3 transposed and halved (n = 0..7, outputs 4..7 zero)
 //   b1 [64], b2 [64], b3 [8] float
 // The row pads keep the B-fragment loads of a warp on 32 distinct banks.
 #pragma once
@@ -58,24 +58,26 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
   return *reinterpret_cast<const uint32_t *>(&v);
 }
 
-// GELU of two FP32 pre-activations, evaluated in packed BF16 arithmetic and
-// returned packed (the next layer's operand).  Each step rounds to BF16:
+// Twice the GELU of two FP32 pre-activations, evaluated in packed BF16
+// arithmetic and returned packed (the next layer's operand).  Each step
+// rounds to BF16:
 //   x = bf16(a), x2 = x*x, t = x2*(c*0.044715) + c, u = x*t,
-//   th = tanh(u) (hardware approximation), h = x*0.5, y = h*th + h
-// with c = sqrt(2/pi) and the constants rounded to BF16; half the
-// instructions and half the SFU operations of the FP32 form.
+//   th = tanh(u) (hardware approximation), y = x*th + x
+// with c = sqrt(2/pi) and the constants rounded to BF16.  y is exactly twice
+// the GELU's h*th + h with h = x*0.5 (a power-of-two scale commutes with each
+// rounding), and the next layer's weights are packed at half scale
+// (pack_mlp_weights), so the products, and everything after them, are those
+// of the GELU itself.  Half the SFU operations of the FP32 form.
 __device__ __forceinline__ uint32_t gelu_bf16x2(float a, float b) {
   const uint32_t kC = 0x3F4C3F4Cu;    // bf16(0.7978845608) = 0.796875, twice
   const uint32_t kC3 = 0x3D123D12u;   // bf16(0.7978845608 * 0.044715) = 0.03564453125, twice
-  const uint32_t kHalf = 0x3F003F00u; // 0.5, twice
   const uint32_t x = pack_bf16(a, b);
-  uint32_t x2, t, u, th, h, y;
+  uint32_t x2, t, u, th, y;
   asm("mul.rn.bf16x2 %0, %1, %1;" : "=r"(x2) : "r"(x));
   asm("fma.rn.bf16x2 %0, %1, %2, %3;" : "=r"(t) : "r"(x2), "r"(kC3), "r"(kC));
   asm("mul.rn.bf16x2 %0, %1, %2;" : "=r"(u) : "r"(x), "r"(t));
   asm("tanh.approx.bf16x2 %0, %1;" : "=r"(th) : "r"(u));
-  asm("mul.rn.bf16x2 %0, %1, %2;" : "=r"(h) : "r"(x), "r"(kHalf));
-  asm("fma.rn.bf16x2 %0, %1, %2, %1;" : "=r"(y) : "r"(h), "r"(th));
+  asm("fma.rn.bf16x2 %0, %1, %2, %1;" : "=r"(y) : "r"(x), "r"(th));
   return y;
 }
 
