@@ -80,7 +80,7 @@ __global__ void __launch_bounds__(kLPB, MCX_LMARCH_MIN_BLOCKS) k_lmarch(PassArgs
     float2 ay = *reinterpret_cast<const float2 *>(m.A1 + m.off);
     float2 az = *reinterpret_cast<const float2 *>(m.A2 + m.off);
     const int dx = m.s ? m.dx1 : m.dx0;
-    const float exv[3] = {ldg1(m.O0 + m.off + dx), ldg1(m.O1 + m.off + dx), ldg1(m.O2 + m.off + dx)};
+    const float exv[3] = {ldo1(m.O0 + m.off + dx), ldo1(m.O1 + m.off + dx), ldo1(m.O2 + m.off + dx)};
     OPair yp, ym;
     load_opair_at<MASK>(m, m.off + m.dyp, m.offp + m.dypp, true, yp);
     load_opair_at<MASK>(m, m.off + m.dym, m.offp + m.dymp, true, ym);

@@ -36,7 +36,7 @@ __device__ __forceinline__ void march_plane(const PassArgs &a, const RepDev &R, 
   float2 ay = *reinterpret_cast<const float2 *>(m.A1 + m.off);
   float2 az = *reinterpret_cast<const float2 *>(m.A2 + m.off);
   const int dx = m.s ? m.dx1 : m.dx0;
-  const float exv[3] = {ldg1(m.O0 + m.off + dx), ldg1(m.O1 + m.off + dx), ldg1(m.O2 + m.off + dx)};
+  const float exv[3] = {ldo1(m.O0 + m.off + dx), ldo1(m.O1 + m.off + dx), ldo1(m.O2 + m.off + dx)};
   OPair yp, ym;
   load_opair_at<MASK>(m, m.off + m.dyp, m.offp + m.dypp, true, yp);
   load_opair_at<MASK>(m, m.off + m.dym, m.offp + m.dymp, true, ym);

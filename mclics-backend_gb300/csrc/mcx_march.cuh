@@ -15,8 +15,8 @@ namespace mcx {
 // that an SM's L1 still held from before the previous pass's writes (the
 // chain then differed from a launch-by-launch run), while L2 loads always
 // see them.
-__device__ __forceinline__ float2 ldg2(const float *p) { return __ldcg(reinterpret_cast<const float2 *>(p)); }
-__device__ __forceinline__ float ldg1(const float *p) { return __ldcg(p); }
+__device__ __forceinline__ float2 ldo2(const float *p) { return __ldcg(reinterpret_cast<const float2 *>(p)); }
+__device__ __forceinline__ float ldo1(const float *p) { return __ldcg(p); }
 
 // Programmatic dependent launch: wait until the preceding grid on the stream
 // has completed and its memory is visible (returns at once when the launch
@@ -79,9 +79,9 @@ __device__ __forceinline__ void dead_unit(const RepDev &R, March &m, int kb, int
 template <bool MASK>
 __device__ __forceinline__ void load_opair_at(const March &m, int off, int offp, bool on, OPair &o) {
   if (on) {
-    o.v[0] = ldg2(m.O0 + off);
-    o.v[1] = ldg2(m.O1 + off);
-    o.v[2] = ldg2(m.O2 + off);
+    o.v[0] = ldo2(m.O0 + off);
+    o.v[1] = ldo2(m.O1 + off);
+    o.v[2] = ldo2(m.O2 + off);
     if (MASK) o.pt = __ldg(reinterpret_cast<const uint16_t *>(m.PO + offp));
   } else {
     o.v[0] = o.v[1] = o.v[2] = make_float2(0.f, 0.f);
