@@ -1,4 +1,5 @@
-"""Statistical parity with the reference's own CPU path on the c1 anneal.
+"""Statistical parity with the reference's own CPU path on the c1 anneal and
+on reduced GHRL configurations.
 
 tests/golden/c1_ll16_anneal.json holds S(T) and E(T) of the reference's
 thermalEvolveN::run (src/evolve_thermal.cpp:30-99) on LL bulk 16^3, random
@@ -57,3 +58,43 @@ def test_c1_anneal_matches_reference_curves():
         z = d / np.maximum(sig, tol / 4)
         chi2.append(float(np.mean(z ** 2)))
     assert max(chi2) < 2.0, chi2
+
+
+def _ghrl_descs(spec, T0, R):
+    geo = spec["geometry"]
+    surf = [dict(anchoring=a, W=W, theta_s=0.0, phi_s=0.0) for a, W in spec["surfaces"]]
+    kw = {k: v for k, v in spec.items() if k not in ("surfaces",)}
+    return [mcx.replica(**kw, T=T0, ang_var=0.5, seed=1 + r, stream=r, surfaces=surf) for r in range(R)], geo
+
+
+@pytest.mark.parametrize("name", ["ghrl_slab16_anneal", "ghrl_sphere16_field_anneal"])
+def test_ghrl_anneals_match_reference_curves(name):
+    """tests/golden/ghrl_*_anneal.json: 32 runs of the reference's CPU thermal
+    loop on a 16^3 GHRL slab (homeotropic, W = 4) and a chiral droplet (planar
+    anchoring, field along z), made by tests/golden/make_ghrl_anneals.py.  The
+    GPU runs 32 replicas with the same protocol; the tolerance is that of the
+    oracle's test on these curves (4 combined standard errors + 2e-3 in S,
+    4e-3 in E)."""
+    g = json.load(open(os.path.join(os.path.dirname(GOLD), name + ".json")))
+    temps, MC, R = g["temps"], g["mct"], 32
+    descs, _ = _ghrl_descs(g["model"], temps[0], R)
+    S = np.zeros((R, len(temps)))
+    E = np.zeros((R, len(temps)))
+    with mcx.Engine(descs) as eng:
+        for r in range(R):
+            eng.init_random(r, 700 + r)
+        for t, T in enumerate(temps):
+            eng.set_temperature(T)
+            eng.sweep(MC)
+            eng.reset_stats()
+            eng.sweep(MC, measure=True)
+            for r in range(R):
+                st = eng.stats(r)
+                S[r, t] = st[mcx.ST_S1] / st[mcx.ST_N]
+                E[r, t] = st[mcx.ST_E1] / st[mcx.ST_N]
+    for key, G, tol in (("S", S, 2e-3), ("E", E, 4e-3)):
+        m, se = G.mean(0), G.std(0, ddof=1) / np.sqrt(R)
+        rm, rse = np.array(g[key + "_mean"]), np.array(g[key + "_sem"])
+        sig = np.hypot(se, rse)
+        bad = np.nonzero(np.abs(m - rm) > 4 * sig + tol)[0]
+        assert len(bad) == 0, [(temps[i], m[i], rm[i], sig[i]) for i in bad]

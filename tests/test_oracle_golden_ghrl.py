@@ -1,0 +1,50 @@
+"""The oracle's red/black chain against the reference's own S(T), E(T) on the
+reduced GHRL configurations (tests/golden/ghrl_*_anneal.json, 32 reference
+runs each, made by tests/golden/make_ghrl_anneals.py): a slab with
+homeotropic anchoring, and a chiral droplet with planar anchoring in a field.
+8 oracle runs per case with the GPU's Philox streams, same protocol; at every
+T the means agree within 4 combined standard errors plus 2e-3 (S) / 4e-3 (E).
+The allowance is wider than c1's: the reference does not renormalise its
+proposals, and its defect textures vary more between runs with anchoring."""
+import functools
+import json
+import multiprocessing as mp
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+R = 8
+
+
+def _model(spec):
+    kw = dict(spec)
+    kw["surfaces"] = [O.Surface(a, W) for a, W in kw.pop("surfaces")]
+    return O.Model(**kw)
+
+
+def _run(seed, spec, temps, mc):
+    m = _model(spec)
+    pt = O.Lattice(m).pt
+    ni0 = O.random_directors(m.n, np.random.default_rng(3000 + seed)).astype(np.float32)
+    ni0[pt == 0] = (0.0, 0.0, 1.0)
+    return O.anneal(m, temps, mc, mc, seed, seed, ni0)
+
+
+@pytest.mark.parametrize("name", ["ghrl_slab16_anneal", "ghrl_sphere16_field_anneal"])
+def test_oracle_ghrl_anneal_matches_reference_curves(name):
+    g = json.load(open(os.path.join(HERE, "golden", name + ".json")))
+    temps = g["temps"]
+    with mp.get_context("spawn").Pool(R) as pool:
+        rows = np.array(pool.map(functools.partial(_run, spec=g["model"], temps=temps, mc=g["mct"]),
+                                 range(1, R + 1)))
+    for col, key, tol in ((1, "S", 2e-3), (2, "E", 4e-3)):
+        G = rows[:, :, col]
+        m, se = G.mean(0), G.std(0, ddof=1) / np.sqrt(R)
+        rm, rse = np.array(g[key + "_mean"]), np.array(g[key + "_sem"])
+        sig = np.hypot(se, rse)
+        bad = np.nonzero(np.abs(m - rm) > 4 * sig + tol)[0]
+        assert len(bad) == 0, [(temps[i], m[i], rm[i], sig[i]) for i in bad]
