@@ -1,4 +1,4 @@
-"""Generates the GHRL golden curves: S(T) and E(T) of the reference's own CPU
+"""Generates the GHRL and Pear golden curves: S(T) and E(T) of the reference's own CPU
 thermal run (thermalEvolveN::run, src/evolve_thermal.cpp:30-99, through the
 reference compiled here as oracle/_ref) on reduced versions of the GHRL
 configurations, over independent runs:
@@ -12,6 +12,8 @@ configurations, over independent runs:
                                    p0 = 20, planar (fg) anchoring W = 1,
                                    field along z (elecA = 1, E = 1);
                                    T = 1.0 -> 0.5, dT = -0.05
+  pear_bulk16_anneal.json          bulk 16^3 periodic, Pear A = 1, B1 = 0.04,
+                                   C = 0.3; T = 1.2 -> 0.6, dT = -0.05
 
 MCT = MCS = 100 per temperature, the step size carried across temperatures,
 generators seeded seed * 104729 + thread (one thread per run).  Initial
@@ -21,7 +23,7 @@ path, but inactive directors enter the all-site field energy).
 
 Run from the repository root, where the reference tree is present
 (`make -C oracle ref` first):
-    python tests/golden/make_ghrl_anneals.py
+    python tests/golden/make_ghrl_anneals.py [case ...]
 """
 from __future__ import annotations
 
@@ -52,6 +54,9 @@ CASES = {
                    potential="ghrl", k11=1.0, k22=0.6, k33=1.4, p0=20.0, elecA=1.0, elecZ=1.0, elecE=1.0,
                    surfaces=[("fg", 1.0)]),
         ti=1.0, tf=0.5, dt=-0.05),
+    "pear_bulk16_anneal": dict(
+        model=dict(nx=16, ny=16, nz=16, potential="pear", A=1.0, B1=0.04, C=0.3, surfaces=[]),
+        ti=1.2, tf=0.6, dt=-0.05),
 }
 
 
@@ -89,7 +94,10 @@ def main():
     if not refproc.available():
         raise SystemExit("oracle/_ref/libref_mcx.so is missing: build it with `make -C oracle ref`")
     ctx = mp.get_context("spawn")
+    only = sys.argv[1:]
     for name, c in CASES.items():
+        if only and name not in only:
+            continue
         temps = temperatures(c["ti"], c["tf"], c["dt"])
         with ctx.Pool(min(RUNS, os.cpu_count() or 1), maxtasksperchild=1) as pool:
             runs = pool.map(one_run, [(name, s) for s in range(1, RUNS + 1)])

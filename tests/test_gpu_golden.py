@@ -61,23 +61,23 @@ def test_c1_anneal_matches_reference_curves():
 
 
 def _ghrl_descs(spec, T0, R):
-    geo = spec["geometry"]
     surf = [dict(anchoring=a, W=W, theta_s=0.0, phi_s=0.0) for a, W in spec["surfaces"]]
     kw = {k: v for k, v in spec.items() if k not in ("surfaces",)}
-    return [mcx.replica(**kw, T=T0, ang_var=0.5, seed=1 + r, stream=r, surfaces=surf) for r in range(R)], geo
+    return [mcx.replica(**kw, T=T0, ang_var=0.5, seed=1 + r, stream=r, surfaces=surf) for r in range(R)]
 
 
-@pytest.mark.parametrize("name", ["ghrl_slab16_anneal", "ghrl_sphere16_field_anneal"])
+@pytest.mark.parametrize("name", ["ghrl_slab16_anneal", "ghrl_sphere16_field_anneal", "pear_bulk16_anneal"])
 def test_ghrl_anneals_match_reference_curves(name):
-    """tests/golden/ghrl_*_anneal.json: 32 runs of the reference's CPU thermal
-    loop on a 16^3 GHRL slab (homeotropic, W = 4) and a chiral droplet (planar
-    anchoring, field along z), made by tests/golden/make_ghrl_anneals.py.  The
+    """tests/golden/{ghrl,pear}_*_anneal.json: 32 runs of the reference's CPU
+    thermal loop on a 16^3 GHRL slab (homeotropic, W = 4), a chiral droplet
+    (planar anchoring, field along z) and bulk Pear, made by
+    tests/golden/make_ghrl_anneals.py.  The
     GPU runs 32 replicas with the same protocol; the tolerance is that of the
     oracle's test on these curves (4 combined standard errors + 2e-3 in S,
     4e-3 in E)."""
     g = json.load(open(os.path.join(os.path.dirname(GOLD), name + ".json")))
     temps, MC, R = g["temps"], g["mct"], 32
-    descs, _ = _ghrl_descs(g["model"], temps[0], R)
+    descs = _ghrl_descs(g["model"], temps[0], R)
     S = np.zeros((R, len(temps)))
     E = np.zeros((R, len(temps)))
     with mcx.Engine(descs) as eng:

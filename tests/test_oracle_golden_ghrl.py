@@ -1,7 +1,8 @@
 """The oracle's red/black chain against the reference's own S(T), E(T) on the
-reduced GHRL configurations (tests/golden/ghrl_*_anneal.json, 32 reference
-runs each, made by tests/golden/make_ghrl_anneals.py): a slab with
-homeotropic anchoring, and a chiral droplet with planar anchoring in a field.
+reduced GHRL and Pear configurations (tests/golden/{ghrl,pear}_*_anneal.json,
+32 reference runs each, made by tests/golden/make_ghrl_anneals.py): a slab
+with homeotropic anchoring, a chiral droplet with planar anchoring in a
+field, and bulk Pear across its transition.
 8 oracle runs per case with the GPU's Philox streams, same protocol; at every
 T the means agree within 4 combined standard errors plus 2e-3 (S) / 4e-3 (E).
 The allowance is wider than c1's: the reference does not renormalise its
@@ -34,7 +35,7 @@ def _run(seed, spec, temps, mc):
     return O.anneal(m, temps, mc, mc, seed, seed, ni0)
 
 
-@pytest.mark.parametrize("name", ["ghrl_slab16_anneal", "ghrl_sphere16_field_anneal"])
+@pytest.mark.parametrize("name", ["ghrl_slab16_anneal", "ghrl_sphere16_field_anneal", "pear_bulk16_anneal"])
 def test_oracle_ghrl_anneal_matches_reference_curves(name):
     g = json.load(open(os.path.join(HERE, "golden", name + ".json")))
     temps = g["temps"]
