@@ -368,6 +368,33 @@ def sweep_uniforms(model: Model, pt: np.ndarray, seed: int, stream: int, sweep: 
     return np.array(out, dtype=np.float64).reshape(-1)
 
 
+def field_sweep(model: Model, T: float, fields: Sequence[float], mct: int, mcs: int, seed: int, stream: int,
+                ni0: np.ndarray, order: str = "redblack") -> np.ndarray:
+    """electricEvolveN::run (src/evolve_electric.cpp:28-90) on the oracle: at
+    temperature T, per field value mct sweeps, then mcs sweeps each followed
+    by E and S; the step size (starting at 0.5) carries across field values.
+    Returns rows (E_field, mean S, mean E)."""
+    lat = Lattice(model)
+    lat.ni[:] = ni0
+    a = np.float32(0.5)
+    sw = 0
+    rows = []
+    for Ef in fields:
+        lat.p.elecE = float(np.float32(Ef))
+        for _ in range(mct):
+            _, a = lat.sweep(T, a, seed, stream, sw, order)
+            sw += 1
+        S1 = E1 = 0.0
+        for _ in range(mcs):
+            _, a = lat.sweep(T, a, seed, stream, sw, order)
+            sw += 1
+            r = lat.measure()
+            S1 += r["S"]
+            E1 += r["E"]
+        rows.append((Ef, S1 / mcs, E1 / mcs))
+    return np.array(rows)
+
+
 def anneal(model: Model, temps: Sequence[float], mct: int, mcs: int, seed: int, stream: int, ni0: np.ndarray,
            order: str = "redblack") -> np.ndarray:
     """thermalEvolveN::run (src/evolve_thermal.cpp:30-99) on the oracle: per

@@ -230,6 +230,10 @@ extern "C" void ref_set_pear(float B1, float C) {
   G->bulk_potential = &Bulk_Energy_Selinger_Pear;
 }
 
+/* The field strength, as electricEvolveN::run steps params->elecE
+ * (src/evolve_electric.cpp:59). */
+extern "C" void ref_set_field(float E) { P->elecE = E; }
+
 /* Re-seeds the per-thread generators as thermalEvolveN::run does
  * (src/evolve_thermal.cpp:40-45): seed * 104729 + thread. */
 extern "C" void ref_seed(unsigned long seed) {

@@ -127,6 +127,30 @@ def _worker(m: dict, ops: List[tuple]) -> List[Any]:
                     S1 += float(L.ref_order(_p(ni), _p(Q), _p(v)))
                 rows.append((T, S1 / mcs, E1 / mcs))
             out.append(np.array(rows))
+        elif kind == "field_sweep":
+            # electricEvolveN::run (src/evolve_electric.cpp:28-90): at T = Ti, per
+            # field value MCT sweeps, then MCS sweeps each followed by
+            # energy_calculator and the order parameter; the step size carries.
+            ni = np.ascontiguousarray(op[1], np.float32).copy()
+            T, fields, mct, mcs, seed, nth = op[2], op[3], op[4], op[5], op[6], op[7]
+            L.ref_seed.argtypes = [C.c_ulong]
+            L.ref_seed(seed)
+            L.ref_set_field.argtypes = [C.c_float]
+            a = C.c_float(0.5)
+            rows = []
+            Q = np.zeros(9, np.float32)
+            v = np.zeros(3, np.float32)
+            for Ef in fields:
+                L.ref_set_field(C.c_float(Ef))
+                for _ in range(mct):
+                    L.ref_sweep(_p(ni), C.c_float(T), C.byref(a), None, 0, nth)
+                S1 = E1 = 0.0
+                for _ in range(mcs):
+                    L.ref_sweep(_p(ni), C.c_float(T), C.byref(a), None, 0, nth)
+                    E1 += float(L.ref_energy(_p(ni)))
+                    S1 += float(L.ref_order(_p(ni), _p(Q), _p(v)))
+                rows.append((Ef, S1 / mcs, E1 / mcs))
+            out.append(np.array(rows))
         elif kind == "order":
             ni = np.ascontiguousarray(op[1], np.float32)
             Q = np.zeros(9, np.float32)

@@ -14,6 +14,9 @@ configurations, over independent runs:
                                    T = 1.0 -> 0.5, dT = -0.05
   pear_bulk16_anneal.json          bulk 16^3 periodic, Pear A = 1, B1 = 0.04,
                                    C = 0.3; T = 1.2 -> 0.6, dT = -0.05
+  ghrl_sphere16_field_sweep.json   the droplet above at T = 0.8 with the field
+                                   stepped E = 0 -> 2.0 by 0.2
+                                   (electricEvolveN::run)
 
 MCT = MCS = 100 per temperature, the step size carried across temperatures,
 generators seeded seed * 104729 + thread (one thread per run).  Initial
@@ -57,11 +60,19 @@ CASES = {
     "pear_bulk16_anneal": dict(
         model=dict(nx=16, ny=16, nz=16, potential="pear", A=1.0, B1=0.04, C=0.3, surfaces=[]),
         ti=1.2, tf=0.6, dt=-0.05),
+    # the droplet configuration's protocol: a field sweep at fixed T
+    # (electricEvolveN::run, src/evolve_electric.cpp:28-90)
+    "ghrl_sphere16_field_sweep": dict(
+        model=dict(nx=16, ny=16, nz=16, geometry="sphere", xbound="free", ybound="free", zbound="free",
+                   potential="ghrl", k11=1.0, k22=0.6, k33=1.4, p0=20.0, elecA=1.0, elecZ=1.0, elecE=0.0,
+                   surfaces=[("fg", 1.0)]),
+        T=0.8, ei=0.0, ef=2.0, de=0.2),
 }
 
 
 def temperatures(ti, tf, dt):
-    """The reference's float loop (src/evolve_thermal.cpp:58)."""
+    """The reference's float loops (src/evolve_thermal.cpp:58,
+    src/evolve_electric.cpp:59)."""
     f = np.float32
     out = []
     T = f(ti)
@@ -86,6 +97,9 @@ def one_run(args):
     rng = np.random.default_rng(2000 + seed)
     ni = O.random_directors(m.n, rng).astype(np.float32)
     ni[pt == 0] = (0.0, 0.0, 1.0)
+    if "T" in c:
+        fields = temperatures(c["ei"], c["ef"], c["de"])
+        return refproc._worker(refproc.model_dict(m), [("field_sweep", ni, c["T"], fields, MCT, MCS, seed, 1)])[0]
     temps = temperatures(c["ti"], c["tf"], c["dt"])
     return refproc._worker(refproc.model_dict(m), [("anneal", ni, temps, MCT, MCS, seed, 1)])[0]
 
@@ -98,13 +112,14 @@ def main():
     for name, c in CASES.items():
         if only and name not in only:
             continue
-        temps = temperatures(c["ti"], c["tf"], c["dt"])
+        temps = temperatures(c["ei"], c["ef"], c["de"]) if "T" in c else temperatures(c["ti"], c["tf"], c["dt"])
         with ctx.Pool(min(RUNS, os.cpu_count() or 1), maxtasksperchild=1) as pool:
             runs = pool.map(one_run, [(name, s) for s in range(1, RUNS + 1)])
-        arr = np.array(runs)  # [run, T, (T, S, E)]
+        arr = np.array(runs)  # [run, step, (T or field, S, E)]
         S, E = arr[:, :, 1], arr[:, :, 2]
         out = {
-            "config": name, "model": c["model"], "mct": MCT, "mcs": MCS, "runs": RUNS, "temps": temps,
+            "config": name, "model": c["model"], "mct": MCT, "mcs": MCS, "runs": RUNS,
+            **({"T": c["T"], "fields": temps} if "T" in c else {"temps": temps}),
             "S_mean": S.mean(0).tolist(), "S_sem": (S.std(0, ddof=1) / np.sqrt(RUNS)).tolist(),
             "E_mean": E.mean(0).tolist(), "E_sem": (E.std(0, ddof=1) / np.sqrt(RUNS)).tolist(),
         }

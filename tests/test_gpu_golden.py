@@ -98,3 +98,34 @@ def test_ghrl_anneals_match_reference_curves(name):
         sig = np.hypot(se, rse)
         bad = np.nonzero(np.abs(m - rm) > 4 * sig + tol)[0]
         assert len(bad) == 0, [(temps[i], m[i], rm[i], sig[i]) for i in bad]
+
+
+def test_droplet_field_sweep_matches_reference_curve():
+    """tests/golden/ghrl_sphere16_field_sweep.json: 32 runs of the reference's
+    electric-field loop (electricEvolveN::run, src/evolve_electric.cpp:28-90)
+    on the chiral GHRL droplet at T = 0.8, field stepped 0 -> 2.0 by 0.2; the
+    GPU runs 32 replicas with the same protocol (per field value 100 sweeps,
+    then 100 measured ones; step size carried)."""
+    g = json.load(open(os.path.join(os.path.dirname(GOLD), "ghrl_sphere16_field_sweep.json")))
+    fields, MC, R = g["fields"], g["mct"], 32
+    descs = _ghrl_descs(g["model"], g["T"], R)
+    S = np.zeros((R, len(fields)))
+    E = np.zeros((R, len(fields)))
+    with mcx.Engine(descs) as eng:
+        for r in range(R):
+            eng.init_random(r, 900 + r)
+        for t, Ef in enumerate(fields):
+            eng.set_field(Ef)
+            eng.sweep(MC)
+            eng.reset_stats()
+            eng.sweep(MC, measure=True)
+            for r in range(R):
+                st = eng.stats(r)
+                S[r, t] = st[mcx.ST_S1] / st[mcx.ST_N]
+                E[r, t] = st[mcx.ST_E1] / st[mcx.ST_N]
+    for key, G, tol in (("S", S, 2e-3), ("E", E, 4e-3)):
+        m, se = G.mean(0), G.std(0, ddof=1) / np.sqrt(R)
+        rm, rse = np.array(g[key + "_mean"]), np.array(g[key + "_sem"])
+        sig = np.hypot(se, rse)
+        bad = np.nonzero(np.abs(m - rm) > 4 * sig + tol)[0]
+        assert len(bad) == 0, [(fields[i], m[i], rm[i], sig[i]) for i in bad]

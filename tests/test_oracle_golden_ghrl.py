@@ -2,7 +2,8 @@
 reduced GHRL and Pear configurations (tests/golden/{ghrl,pear}_*_anneal.json,
 32 reference runs each, made by tests/golden/make_ghrl_anneals.py): a slab
 with homeotropic anchoring, a chiral droplet with planar anchoring in a
-field, and bulk Pear across its transition.
+field, bulk Pear across its transition, and the droplet's field sweep at
+fixed T (electricEvolveN::run).
 8 oracle runs per case with the GPU's Philox streams, same protocol; at every
 T the means agree within 4 combined standard errors plus 2e-3 (S) / 4e-3 (E).
 The allowance is wider than c1's: the reference does not renormalise its
@@ -27,20 +28,23 @@ def _model(spec):
     return O.Model(**kw)
 
 
-def _run(seed, spec, temps, mc):
+def _run(seed, spec, steps, mc, T):
     m = _model(spec)
     pt = O.Lattice(m).pt
     ni0 = O.random_directors(m.n, np.random.default_rng(3000 + seed)).astype(np.float32)
     ni0[pt == 0] = (0.0, 0.0, 1.0)
-    return O.anneal(m, temps, mc, mc, seed, seed, ni0)
+    if T is not None:  # a field sweep at fixed T
+        return O.field_sweep(m, T, steps, mc, mc, seed, seed, ni0)
+    return O.anneal(m, steps, mc, mc, seed, seed, ni0)
 
 
-@pytest.mark.parametrize("name", ["ghrl_slab16_anneal", "ghrl_sphere16_field_anneal", "pear_bulk16_anneal"])
+@pytest.mark.parametrize("name", ["ghrl_slab16_anneal", "ghrl_sphere16_field_anneal", "pear_bulk16_anneal",
+                                  "ghrl_sphere16_field_sweep"])
 def test_oracle_ghrl_anneal_matches_reference_curves(name):
     g = json.load(open(os.path.join(HERE, "golden", name + ".json")))
-    temps = g["temps"]
+    temps = g.get("temps", g.get("fields"))
     with mp.get_context("spawn").Pool(R) as pool:
-        rows = np.array(pool.map(functools.partial(_run, spec=g["model"], temps=temps, mc=g["mct"]),
+        rows = np.array(pool.map(functools.partial(_run, spec=g["model"], steps=temps, mc=g["mct"], T=g.get("T")),
                                  range(1, R + 1)))
     for col, key, tol in ((1, "S", 2e-3), (2, "E", 4e-3)):
         G = rows[:, :, col]
