@@ -275,7 +275,9 @@ def _assert_same(out_a, out_b):
         assert np.array_equal(sa, sb)
         assert ta[mcx.ST_ANG_VAR] == tb[mcx.ST_ANG_VAR]
         assert ta[mcx.ST_ACC] == tb[mcx.ST_ACC]
-        assert ta[mcx.ST_S1] == pytest.approx(tb[mcx.ST_S1], rel=1e-6)
+        # S sums: FP32 partial sums in a different order per kernel; near-zero S
+        # (disordered states of big lattices) needs an absolute allowance
+        assert ta[mcx.ST_S1] == pytest.approx(tb[mcx.ST_S1], rel=1e-6, abs=1e-7 * ta[mcx.ST_N])
         assert ta[mcx.ST_E1] == pytest.approx(tb[mcx.ST_E1], rel=1e-6)
 
 
@@ -392,3 +394,24 @@ def test_autotune_keeps_state_and_results():
         b.sweep(40, measure=True)
         assert np.array_equal(a.get_state(0), b.get_state(0))
         assert a.stats(0)[mcx.ST_ANG_VAR] == b.stats(0)[mcx.ST_ANG_VAR]
+
+
+@pytest.mark.parametrize("dims", [(512, 512, 512), (1024, 1024, 130)])
+def test_large_lattice_kernels_agree(dims):
+    """Lattices of 134 M and 136 M sites (1.6 GB of directors): the z-march,
+    in the autotuner's shape and in the prefetching form, and the direct
+    pass stay bit-identical, so no offset or Philox counter overflows at the
+    largest sizes the configurations use and beyond."""
+    nx, ny, nz = dims
+    d = mcx.replica(nx=nx, ny=ny, nz=nz, potential="ll", T=1.0, seed=17, stream=3)
+    outs = []
+    for kind in ("march", "march_async", "direct"):
+        with mcx.Engine([d]) as eng:
+            eng.init_random(0, 5)
+            eng.pass_kind = kind
+            if kind == "march":
+                eng.autotune()
+            eng.sweep(2, measure=True)
+            outs.append((eng.get_state(0), eng.stats(0)))
+    _assert_same(outs[0:1], outs[1:2])
+    _assert_same(outs[0:1], outs[2:3])
