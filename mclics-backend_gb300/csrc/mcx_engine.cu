@@ -75,7 +75,8 @@ struct mcx_engine {
   bool tmarch = false;  // the z-march with rows staged by bulk copies (unmasked lattices)
   bool amarch = false;  // the z-march with a per-thread cp.async prefetch (unmasked LL / GHRL)
   bool pmarch = false;  // the z-march as one cooperative launch per run of sweeps (grid barriers)
-  // per replica of a masked batch: row j + ny * k holds an active site (empty: unknown)
+  // per replica of a masked batch, row j + ny * k: 0 no active site, 1 only
+  // bulk sites (point type 1), 2 anything else (empty: unknown)
   std::vector<std::vector<uint8_t>> rowact;
   // learned-proposal z-march: its own units (128 pairs x kLearnPlanes planes)
   std::vector<int4> lunits;
@@ -249,14 +250,16 @@ static void effective_bounds(mcx_replica_desc &d) {
 // the column blocks of all replicas are cut into chunks of near-equal depth
 // (sizes differ by at most one plane) so that the units fill max(1, -march_k)
 // waves, which keeps the last wave from running mostly idle.
-// A unit of a masked replica is dead when its rows and planes, and the rows
-// and planes next to them, hold no active site (kUnitDead).
-static bool unit_dead(const mcx_engine *e, const int4 &u) {
+// The class of a unit of a masked replica from its rows and planes and the
+// rows and planes next to them: kUnitDead when none holds an active site,
+// kUnitBulk when all hold bulk sites only, 0 otherwise.
+static int unit_class(const mcx_engine *e, const int4 &u) {
   const std::vector<uint8_t> &act = e->rowact[u.x];
-  if (act.empty()) return false;
+  if (act.empty()) return 0;
   const RepDev &R = e->rep[u.x];
   const int pend = std::min(u.y + e->march_nt, R.hp * R.ny);
   const int j0 = u.y / R.hp, j1 = (pend - 1) / R.hp, nk = u.w & kUnitPlanes;
+  unsigned seen = 0;  // bit c: a row of class c
   for (int k = u.z - 1; k <= u.z + nk; k++) {
     int kk = k;
     if (kk < 0 || kk >= R.nz) {
@@ -269,14 +272,16 @@ static bool unit_dead(const mcx_engine *e, const int4 &u) {
         if (R.yb != BOUND_PERIODIC) continue;
         jj = (jj + R.ny) % R.ny;
       }
-      if (act[(size_t)jj + (size_t)R.ny * kk]) return false;
+      seen |= 1u << act[(size_t)jj + (size_t)R.ny * kk];
     }
   }
-  return true;
+  return seen == 1u ? kUnitDead : (seen == 2u ? kUnitBulk : 0);
 }
 
+static bool unit_dead(const mcx_engine *e, const int4 &u) { return unit_class(e, u) == kUnitDead; }
+
 static void mark_dead_units(mcx_engine *e) {
-  for (int4 &u : e->units) u.w = (u.w & kUnitPlanes) | (unit_dead(e, u) ? kUnitDead : 0);
+  for (int4 &u : e->units) u.w = (u.w & kUnitPlanes) | unit_class(e, u);
 }
 
 static void plan_march(mcx_engine *e) {
@@ -650,12 +655,14 @@ extern "C" mcx_status mcx_set_mask(mcx_engine *e, int r, const int *pt, const fl
   // which rows hold an active site: z-march units far from every one skip their updates
   std::vector<uint8_t> &act = e->rowact[r];
   act.assign((size_t)R.ny * R.nz, 0);
-  for (long row = 0; row < (long)R.ny * R.nz; row++)
-    for (int i = 0; i < R.nx; i++)
-      if (pt[row * R.nx + i]) {
-        act[row] = 1;
-        break;
-      }
+  for (long row = 0; row < (long)R.ny * R.nz; row++) {
+    bool any = false, bulk = true;
+    for (int i = 0; i < R.nx; i++) {
+      any |= pt[row * R.nx + i] != 0;
+      bulk &= pt[row * R.nx + i] == 1;
+    }
+    act[row] = bulk ? 1 : (any ? 2 : 0);
+  }
   if (e->d_units && !e->units.empty()) {
     mark_dead_units(e);
     CK(e, cudaMemcpyAsync(e->d_units, e->units.data(), sizeof(int4) * e->units.size(), cudaMemcpyHostToDevice,

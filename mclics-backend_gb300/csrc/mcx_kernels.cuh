@@ -34,7 +34,12 @@ enum PassMode : int {
 // energy of its sites in measured sweeps (what the full update adds for an
 // inactive site).
 constexpr int kUnitDead = 1 << 30;
-constexpr int kUnitPlanes = kUnitDead - 1;
+// kUnitBulk marks a unit of a masked replica whose rows and planes, and the
+// rows and planes next to them, hold only bulk sites (point type 1): it runs
+// the unmasked update, which gives the same result there without the mask's
+// loads and weights.
+constexpr int kUnitBulk = 1 << 29;
+constexpr int kUnitPlanes = kUnitBulk - 1;
 
 struct PassArgs {
   const RepDev *reps;

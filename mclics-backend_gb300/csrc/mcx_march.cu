@@ -54,6 +54,42 @@ __device__ __forceinline__ void march_plane(const PassArgs &a, const RepDev &R, 
   *reinterpret_cast<float2 *>(m.A2 + m.off) = az;
 }
 
+// The march of one unit's chunk of planes kb..ke-1 (everything after the
+// dependency wait).
+template <int POT, bool MASK, bool FIELD, int MODE, bool PER>
+__device__ __forceinline__ void march_chunk(const PassArgs &a, const RepDev &R, int c, March &m, int kb, int ke,
+                                            const RepState *S, unsigned &acc, float qs[kQ]) {
+  const int nz = R.nz;
+  const bool zper = R.zb == BOUND_PERIODIC;
+  const uint32_t seed = R.seed, stream = R.stream;
+  const unsigned long long sw = S->sweep;
+  const float ang = S->ang_var, invT = 1.0f / S->T;
+  // the z pipeline: opposite pairs of this column at planes k-1, k, k+1
+  OPair om, o0, op;
+  const bool zm0 = kb > 0 || zper;
+  {
+    const int wrap = kb == 0 ? nz : 0;  // plane -1 is plane nz-1 when z is periodic
+    load_opair_at<MASK>(m, m.off + (wrap - 1) * m.dz, m.offp + (wrap - 1) * m.dzp, zm0, om);
+    load_opair_at<MASK>(m, m.off, m.offp, true, o0);
+  }
+  bool zm = zm0;
+#pragma unroll 1
+  for (int k = kb; k < ke; k++) {
+    const bool zp = k + 1 < nz || zper;
+    const int up = k + 1 < nz ? 1 : 1 - nz;
+    load_opair_at<MASK>(m, m.off + up * m.dz, m.offp + up * m.dzp, zp, op);
+    march_plane<POT, MASK, FIELD, MODE, PER>(a, R, c, m, om, o0, op, zp, zm, seed, stream, sw, ang, invT, acc, qs);
+    om = o0;
+    o0 = op;
+    zm = true;
+    m.off += m.dz;
+    m.offp += m.dzp;
+    m.pid += m.dpid;
+    m.row += R.ny;
+    m.s ^= 1;
+  }
+}
+
 template <int POT, bool MASK, bool FIELD, int MODE, int NT, bool PER>
 __global__ void __launch_bounds__(NT, march_min_blocks<POT, MASK, NT>()) k_march(PassArgs a) {
   static_assert(MODE == MODE_SWEEP || MODE == MODE_SWEEP_MEASURE, "sweep modes only");
@@ -67,46 +103,19 @@ __global__ void __launch_bounds__(NT, march_min_blocks<POT, MASK, NT>()) k_march
   for (int q = 0; q < kQ; q++) qs[q] = 0.f;
   const int p = u.y + (int)threadIdx.x;
   if (p < R.hp * R.ny) {
-    const int nz = R.nz;
     March m;
     march_init<MASK>(a, R, c, p, u.z, m);
-    const bool zper = R.zb == BOUND_PERIODIC;
     const int kb = u.z, ke = u.z + (u.w & kUnitPlanes);
-    const uint32_t seed = R.seed, stream = R.stream;
     // everything above depends only on constants; the state and the
     // directors may still be written by the previous pass (programmatic
     // dependent launch lets this grid start while that one drains)
     grid_dependency_wait(m);
-    if (MASK && (u.w & kUnitDead)) {
+    if (MASK && (u.w & kUnitDead))
       dead_unit<FIELD, MODE>(R, m, kb, ke, qs);
-    } else {
-    const unsigned long long sw = S->sweep;
-    const float ang = S->ang_var, invT = 1.0f / S->T;
-    // the z pipeline: opposite pairs of this column at planes k-1, k, k+1
-    OPair om, o0, op;
-    const bool zm0 = kb > 0 || zper;
-    {
-      const int wrap = kb == 0 ? nz : 0;  // plane -1 is plane nz-1 when z is periodic
-      load_opair_at<MASK>(m, m.off + (wrap - 1) * m.dz, m.offp + (wrap - 1) * m.dzp, zm0, om);
-      load_opair_at<MASK>(m, m.off, m.offp, true, o0);
-    }
-    bool zm = zm0;
-#pragma unroll 1
-    for (int k = kb; k < ke; k++) {
-      const bool zp = k + 1 < nz || zper;
-      const int up = k + 1 < nz ? 1 : 1 - nz;
-      load_opair_at<MASK>(m, m.off + up * m.dz, m.offp + up * m.dzp, zp, op);
-      march_plane<POT, MASK, FIELD, MODE, PER>(a, R, c, m, om, o0, op, zp, zm, seed, stream, sw, ang, invT, acc, qs);
-      om = o0;
-      o0 = op;
-      zm = true;
-      m.off += m.dz;
-      m.offp += m.dzp;
-      m.pid += m.dpid;
-      m.row += R.ny;
-      m.s ^= 1;
-    }
-    }
+    else if (MASK && (u.w & kUnitBulk))  // only bulk sites around: the unmasked update
+      march_chunk<POT, false, FIELD, MODE, false>(a, R, c, m, kb, ke, S, acc, qs);
+    else
+      march_chunk<POT, MASK, FIELD, MODE, PER>(a, R, c, m, kb, ke, S, acc, qs);
   }
   grid_dependency_wait();    // threads without a pair reach here without having waited
   grid_launch_dependents();  // the next pass may start its set-up now

@@ -415,3 +415,25 @@ def test_large_lattice_kernels_agree(dims):
             outs.append((eng.get_state(0), eng.stats(0)))
     _assert_same(outs[0:1], outs[1:2])
     _assert_same(outs[0:1], outs[2:3])
+
+
+@pytest.mark.parametrize("pot", ["ghrl", "ll"])
+def test_bulk_and_dead_units_agree_with_direct_pass(pot):
+    """Masked lattices whose z-march units include bulk units (only point
+    type 1 around: the unmasked update) and dead units (no active site
+    around): a deep slab and a small droplet in a large box.  Bit-identical
+    to the direct pass."""
+    slab = O.Model(nx=16, ny=16, nz=48, geometry="slab", potential=pot, k11=1.0, k22=0.8, k33=1.2, elecA=0.4,
+                   elecZ=1.0, elecE=1.0, surfaces=[O.Surface("homeotropic", 4.0), O.Surface("homeotropic", 4.0)])
+    drop = O.Model(nx=32, ny=32, nz=32, geometry="sphere", potential=pot, k11=1.0, k22=0.6, k33=1.4, p0=20,
+                   elecA=0.3, elecZ=1.0, elecE=1.5, radius=6.0, surfaces=[O.Surface("fg", 1.0)])
+    for m in (slab, drop):
+        d = desc_from_model(m, T=0.9, seed=31, stream=5)
+        pt = O.Lattice(m).pt
+
+        def setup(eng):
+            eng.set_state(0, random_state(m, pt, np.random.default_rng(13)))
+
+        ref = _run_kernel([d], setup, "direct", 0, 0)
+        for block, planes in ((64, 8), (128, 4), (64, -2)):
+            _assert_same(ref, _run_kernel([d], setup, "march", block, planes))
