@@ -253,11 +253,11 @@ static void effective_bounds(mcx_replica_desc &d) {
 // The class of a unit of a masked replica from its rows and planes and the
 // rows and planes next to them: kUnitDead when none holds an active site,
 // kUnitBulk when all hold bulk sites only, 0 otherwise.
-static int unit_class(const mcx_engine *e, const int4 &u) {
+static int unit_class(const mcx_engine *e, const int4 &u, int nt) {
   const std::vector<uint8_t> &act = e->rowact[u.x];
   if (act.empty()) return 0;
   const RepDev &R = e->rep[u.x];
-  const int pend = std::min(u.y + e->march_nt, R.hp * R.ny);
+  const int pend = std::min(u.y + nt, R.hp * R.ny);
   const int j0 = u.y / R.hp, j1 = (pend - 1) / R.hp, nk = u.w & kUnitPlanes;
   unsigned seen = 0;  // bit c: a row of class c
   for (int k = u.z - 1; k <= u.z + nk; k++) {
@@ -278,10 +278,16 @@ static int unit_class(const mcx_engine *e, const int4 &u) {
   return seen == 1u ? kUnitDead : (seen == 2u ? kUnitBulk : 0);
 }
 
-static bool unit_dead(const mcx_engine *e, const int4 &u) { return unit_class(e, u) == kUnitDead; }
+static bool unit_dead(const mcx_engine *e, const int4 &u) { return unit_class(e, u, e->march_nt) == kUnitDead; }
 
+// Flags of the z-march units and of the learned z-march's units (which only
+// use kUnitDead).
 static void mark_dead_units(mcx_engine *e) {
-  for (int4 &u : e->units) u.w = (u.w & kUnitPlanes) | unit_class(e, u);
+  for (int4 &u : e->units) u.w = (u.w & kUnitPlanes) | unit_class(e, u, e->march_nt);
+  for (int4 &u : e->lunits) {
+    const int cls = unit_class(e, u, lmarch_block_threads());
+    u.w = (u.w & kUnitPlanes) | (cls == kUnitDead ? kUnitDead : 0);
+  }
 }
 
 static void plan_march(mcx_engine *e) {
@@ -663,12 +669,14 @@ extern "C" mcx_status mcx_set_mask(mcx_engine *e, int r, const int *pt, const fl
     }
     act[row] = bulk ? 1 : (any ? 2 : 0);
   }
-  if (e->d_units && !e->units.empty()) {
-    mark_dead_units(e);
+  mark_dead_units(e);
+  if (e->d_units && !e->units.empty())
     CK(e, cudaMemcpyAsync(e->d_units, e->units.data(), sizeof(int4) * e->units.size(), cudaMemcpyHostToDevice,
                           e->stream));
-    drop_graphs(e);
-  }
+  if (e->d_lunits && !e->lunits.empty())
+    CK(e, cudaMemcpyAsync(e->d_lunits, e->lunits.data(), sizeof(int4) * e->lunits.size(), cudaMemcpyHostToDevice,
+                          e->stream));
+  drop_graphs(e);
   CK(e, cudaStreamSynchronize(e->stream));
   return MCX_OK;
 }
@@ -947,6 +955,7 @@ static mcx_status plan_lmarch(mcx_engine *e) {
         R.lcta++;
       }
   }
+  for (int4 &u : e->lunits) u.w |= unit_class(e, u, nt) == kUnitDead ? kUnitDead : 0;
   cudaFree(e->d_lunits);
   e->d_lunits = nullptr;
   CK(e, cudaMalloc(&e->d_lunits, sizeof(int4) * e->lunits.size()));

@@ -60,6 +60,9 @@ __global__ void __launch_bounds__(kLPB, MCX_LMARCH_MIN_BLOCKS) k_lmarch(PassArgs
   for (int q = 0; q < kQ; q++) qs[q] = 0.f;
   __syncthreads();  // weights in shared memory
   grid_dependency_wait(m);
+  if (MASK && (u.w & kUnitDead)) {  // no active site in or next to the unit: field energies only
+    if (valid) dead_unit<FIELD, MODE>(R, m, kb, ke, qs);
+  } else {
   const unsigned long long sw = S->sweep;
   const float T = S->T, invT = 1.0f / S->T;
   OPair om, o0, op;
@@ -172,6 +175,7 @@ __global__ void __launch_bounds__(kLPB, MCX_LMARCH_MIN_BLOCKS) k_lmarch(PassArgs
     m.pid += m.dpid;
     m.row += R.ny;
     m.s ^= 1;
+  }
   }
   grid_launch_dependents();
   flush_replica<kLPB, MODE>(a, r, 1, (unsigned)R.lcta, acc, qs, MASK);
