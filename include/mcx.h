@@ -209,12 +209,19 @@ long long mcx_kernel_launches(const mcx_engine *eng);
  * 0 the direct pass (each thread loads its neighbours from global memory).
  * The direct pass is the default (it measures faster on the lattices
  * benchmarked so far); the staged pass needs every replica's tile to fit in
- * shared memory.  Both give bit-identical results. */
+ * shared memory.  Both compute the same update (see mcx_set_pass). */
 mcx_status mcx_set_staged(mcx_engine *eng, int on);
 int mcx_get_staged(const mcx_engine *eng);
 
-/* The kernel that runs the plain proposal's sweeps (all give bit-identical
- * results):
+/* The kernel that runs the plain proposal's sweeps.  All compute the same
+ * update from the same Philox counters, and each is deterministic run to
+ * run; two forms agree bit for bit except where a decision lies within an
+ * ulp of its threshold (about one in 10^7-10^8 updates: the compiler fuses
+ * multiply-adds per kernel), after which their trajectories part but sample
+ * the same states.  Pin the form and shape (mcx_set_pass,
+ * mcx_set_march_shape) for runs that must repeat bit for bit: the
+ * autotuner's choice depends on timing.
+ *
  *   MCX_PASS_MARCH   the default: a CTA marches a block of same-colour site
  *                    pairs of one z-plane through a chunk of planes, keeping
  *                    the z neighbours in registers;

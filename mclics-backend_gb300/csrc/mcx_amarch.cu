@@ -1,7 +1,8 @@
 // mcx_amarch.cu -- the z-march of the plain proposal with a per-thread
 // cp.async prefetch of the next plane's neighbourhood (k_amarch), and its
 // launchers.  Same work units, Philox counters and pair update as k_march
-// (mcx_march.cu), so the two are bit-identical; this form hides each plane's
+// (mcx_march.cu), so the two agree bit for bit except at decisions within an
+// ulp of their threshold (see mcx_march.cu); this form hides each plane's
 // load latency behind the arithmetic of the plane before it.
 #include <cuda_runtime.h>
 
@@ -19,7 +20,7 @@ namespace mcx {
 // copied, so cp.async.wait_group alone orders copies and reads: no block
 // barrier, no registers held by loads in flight.  Slots are structure-of-
 // arrays ([stage][slot][thread]), so the reads are conflict-free.  Unmasked
-// lattices; bit-identical to k_march (same inputs to update_pair).
+// lattices; the same inputs to update_pair as k_march.
 // ---------------------------------------------------------------------------
 constexpr int kAF2 = 12;  // float2 slots per stage: own, y+1, y-1, plane k+1 opposite (x 3 components)
 constexpr int kAF1 = 3;   // float slots per stage: the extra x site (3 components)

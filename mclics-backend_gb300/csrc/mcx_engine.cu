@@ -829,7 +829,7 @@ static bool persistent(const mcx_engine *e) {
 }
 
 static mcx_status run_sweeps(mcx_engine *e, int n, int m) {
-  if (persistent(e) && pmarch_fits(e)) {  // otherwise the register march below (bit-identical)
+  if (persistent(e) && pmarch_fits(e)) {  // otherwise the register march below (the same update)
     PassArgs pa = pass_args(e);
     for (int done = 0; done < n;) {
       const int k = std::min(n - done, kPersistentSweeps);

@@ -14,9 +14,11 @@
 //             (weights and one input/output tile per warp), four CTAs of 128
 //             threads per SM at 128 registers.
 //
-// Results are bit-identical to the learned direct pass (k_pass<LEARN>): the
+// It computes what the learned direct pass (k_pass<LEARN>) computes: the
 // same rows reach the network, the same per-site Philox counters drive the
-// draws.
+// draws.  Results agree bit for bit except where a decision lies within an
+// ulp of its threshold: the compiler fuses multiply-adds per kernel, so such
+// a decision (about one in 10^7-10^8 updates) can go the other way.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 

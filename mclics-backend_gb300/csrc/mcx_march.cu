@@ -16,8 +16,14 @@
 //            geometry, its y rows and its x extras are computed once per
 //            chunk; the Philox key schedule once per thread.
 //
-// Results are bit-identical to the other passes (same site_update, same
-// Philox counter: pair index row * hp + q, sweep, colour).
+// It computes what the other passes compute (same site_update, same Philox
+// counter: pair index row * hp + q, sweep, colour).  Results agree bit for
+// bit except where a decision lies within an ulp of its threshold: each
+// kernel inlines the update into different code and the compiler fuses its
+// multiply-adds (a*b + c*d as fma(a, b, c*d) or fma(c, d, a*b)) per kernel,
+// so about one decision in 10^7-10^8 updates can go the other way, after
+// which the trajectories part but sample the same states.  Each form is
+// deterministic run to run.
 #include <cuda_runtime.h>
 
 #include "mcx_march.cuh"
@@ -45,6 +51,9 @@ __device__ __forceinline__ void march_plane(const PassArgs &a, const RepDev &R, 
   if (MASK) {
     pself = __ldg(reinterpret_cast<const uint16_t *>(m.PA + m.offp));
     pex = __ldg(m.PO + m.offp + dx);
+    // two inactive sites: nothing moves, and an unmeasured sweep adds nothing
+    // (a warp of such pairs skips the draw and the arithmetic)
+    if (MODE == MODE_SWEEP && pself == 0) return;
   }
   update_pair<POT, MASK, FIELD, MODE, PER>(a, R, c, m.s, m.hasB, m.ee0, m.ee1, m.eyp, m.eym, o0, yp, ym, op, om, exv,
                                            pself, pex, zp, zm, m.pid, m.off, seed, stream, sw, ang, invT, ax, ay, az,

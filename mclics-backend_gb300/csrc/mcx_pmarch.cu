@@ -22,8 +22,9 @@
 // of the launch read what other CTAs wrote in earlier ones, and L1 is not
 // coherent between SMs.  Point types and normals never change and keep the
 // read-only path.  Per pass the work is that of k_march (mcx_march.cu) with
-// the same units, Philox counters and pair update, so results are
-// bit-identical to it.
+// the same units, Philox counters and pair update, so results agree with it
+// bit for bit except at decisions within an ulp of their threshold (see
+// mcx_march.cu).
 #include <cuda_runtime.h>
 
 #include "mcx_march.cuh"

@@ -146,3 +146,33 @@ def test_learned_march_equals_learned_direct_pass(name):
     assert np.array_equal(sa, sb)
     assert ta[mcx.ST_ANG_VAR] == tb[mcx.ST_ANG_VAR] and ta[mcx.ST_ACC] == tb[mcx.ST_ACC]
     assert ta[mcx.ST_S1] == pytest.approx(tb[mcx.ST_S1], rel=1e-6)
+
+
+def test_learned_forms_agree_over_long_runs():
+    """16 chiral droplets in a field, 50 + 50 measured learned sweeps: the
+    learned z-march and the learned direct pass may part after a decision
+    within an ulp of its threshold (their multiply-adds are fused by the
+    compiler in each kernel), but they sample the same states: replica-averaged
+    S and E agree within their statistical error."""
+    m = O.Model(nx=64, ny=64, nz=64, geometry="sphere", xbound="free", ybound="free", zbound="free",
+                potential="ghrl", k11=1.0, k22=0.6, k33=1.4, p0=20.0, elecA=1.0, elecZ=1.0, elecE=0.5, radius=26.0,
+                surfaces=[O.Surface("fg", 1.0)])
+    descs = [desc_from_model(m, T=0.8, seed=500 + q, stream=q) for q in range(16)]
+    params = _weights(4)
+    means = []
+    for kind in ("march", "direct"):
+        with mcx.Engine(descs) as eng:
+            eng.pass_kind = kind
+            for q in range(16):
+                eng.init_random(q, 11 + q)
+            eng.set_mlp(M.pack_weights(params))
+            eng.set_proposal("vmf_mlp")
+            eng.sweep(50)
+            eng.reset_stats()
+            eng.sweep(50, measure=True)
+            st = [eng.stats(q) for q in range(16)]
+        means.append((np.array([t[mcx.ST_S1] / t[mcx.ST_N] for t in st]),
+                      np.array([t[mcx.ST_E1] / t[mcx.ST_N] for t in st])))
+    for a, b in zip(*means):
+        se = np.sqrt(a.var(ddof=1) / len(a) + b.var(ddof=1) / len(b))
+        assert abs(a.mean() - b.mean()) <= 5 * se + 1e-6 * abs(a.mean()), (a.mean(), b.mean(), se)

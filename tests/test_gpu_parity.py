@@ -437,3 +437,65 @@ def test_bulk_and_dead_units_agree_with_direct_pass(pot):
         ref = _run_kernel([d], setup, "direct", 0, 0)
         for block, planes in ((64, 8), (128, 4), (64, -2)):
             _assert_same(ref, _run_kernel([d], setup, "march", block, planes))
+
+
+LONG_RUNS = {
+    # chiral GHRL droplets with planar anchoring in a field: masked units of
+    # every kind (surface, bulk, dead)
+    "ghrl_droplets_field": dict(nx=64, ny=64, nz=64, geometry="sphere", xbound="free", ybound="free", zbound="free",
+                                potential="ghrl", k11=1.0, k22=0.6, k33=1.4, p0=20.0, elecA=1.0, elecZ=1.0,
+                                elecE=0.5, radius=26.0, surfaces=[O.Surface("fg", 1.0)]),
+    # unmasked periodic GHRL in a field: the prefetching z-march applies
+    "ghrl_bulk_field": dict(nx=48, ny=48, nz=48, potential="ghrl", k11=1.0, k22=0.8, k33=1.2, p0=15.0, elecA=0.5,
+                            elecX=0.3, elecZ=1.0, elecE=1.0),
+    "pear_bulk": dict(nx=48, ny=48, nz=48, potential="pear", A=1.0, B1=0.04, C=0.3),
+}
+LONG_KERNELS = [("march", 128, 8), ("march", 256, 0), ("march_tma", 128, 8), ("march_async", 256, 0),
+                ("march_persistent", 256, 0), ("staged", 0, 0)]
+
+
+def _replica_means(out):
+    """Per-replica mean S and E from measured-sweep sums."""
+    S = np.array([st[mcx.ST_S1] / st[mcx.ST_N] for _, st in out])
+    E = np.array([st[mcx.ST_E1] / st[mcx.ST_N] for _, st in out])
+    return S, E
+
+
+def _assert_same_distribution(ref, out):
+    for a, b in zip(_replica_means(ref), _replica_means(out)):
+        se = np.sqrt(a.var(ddof=1) / len(a) + b.var(ddof=1) / len(b))
+        assert abs(a.mean() - b.mean()) <= 5 * se + 1e-6 * abs(a.mean()), (a.mean(), b.mean(), se)
+
+
+@pytest.mark.parametrize("name", list(LONG_RUNS))
+def test_pass_forms_agree_over_long_runs(name):
+    """16 replicas, 100 + 100 measured sweeps (about 10^8 site updates per
+    form).  The forms inline the same update into different code, and the
+    compiler may fuse its multiply-adds differently in each, so about one
+    decision in 10^7-10^8 that lies within an ulp of its threshold can go
+    the other way and the trajectories part.  What must hold over long runs
+    is that every form samples the same states: replica-averaged S and E
+    agree within their statistical error."""
+    m = O.Model(**LONG_RUNS[name])
+    descs = [desc_from_model(m, T=0.8, seed=500 + q, stream=q) for q in range(16)]
+
+    def run(kind, block, planes):
+        with mcx.Engine(descs) as eng:
+            try:
+                eng.pass_kind = kind
+            except mcx.McxError:
+                return None  # not every batch fits every form
+            if kind.startswith("march"):
+                eng.set_march_shape(block, planes)
+            for q in range(16):
+                eng.init_random(q, 11 + q)
+            eng.sweep(100)
+            eng.reset_stats()
+            eng.sweep(100, measure=True)
+            return [(eng.get_state(q), eng.stats(q)) for q in range(16)]
+
+    ref = run("direct", 0, 0)
+    for kind, block, planes in LONG_KERNELS:
+        out = run(kind, block, planes)
+        if out is not None:
+            _assert_same_distribution(ref, out)
