@@ -499,3 +499,82 @@ def test_pass_forms_agree_over_long_runs(name):
         out = run(kind, block, planes)
         if out is not None:
             _assert_same_distribution(ref, out)
+
+
+def test_pass_forms_part_only_at_near_ties():
+    """Where the z-march and the direct pass part on a long run, the first
+    decision that differs is a near-tie: u within the parity tests' tie band
+    of exp(-dE/T), dE evaluated in FP64 by the oracle.  Chiral droplets in a
+    field (8 replicas of 96^3, r = 40), stepped one sweep at a time until the
+    acceptance counts differ (up to 300 sweeps); the parted replica is then
+    re-run alone to the sweep before, where both forms still agree, and that
+    one sweep is analysed site by site."""
+    m = O.Model(nx=96, ny=96, nz=96, geometry="sphere", xbound="free", ybound="free", zbound="free",
+                potential="ghrl", k11=1.0, k22=0.6, k33=1.4, p0=20.0, elecA=1.0, elecZ=1.0, elecE=0.5,
+                radius=40.0, surfaces=[O.Surface("fg", 1.0)])
+    T, R = 0.8, 8
+    descs = [desc_from_model(m, T=T, seed=500 + q, stream=q) for q in range(R)]
+    kinds = ("march", "direct")
+    engs = []
+    try:
+        for kind in kinds:
+            eng = mcx.Engine(descs)
+            eng.pass_kind = kind
+            for q in range(R):
+                eng.init_random(q, 11 + q)
+            engs.append(eng)
+        parted = None
+        for n in range(1, 301):
+            for eng in engs:
+                eng.sweep(1)
+            acc = [[eng.stats(q)[mcx.ST_ACC] for q in range(R)] for eng in engs]
+            diff = [q for q in range(R) if acc[0][q] != acc[1][q]]
+            if diff:
+                parted = (n, diff[0])
+                break
+    finally:
+        for eng in engs:
+            eng.close()
+    if parted is None:
+        return  # the forms agreed over the whole run: no parting to analyse
+    n, q = parted
+    states = {}
+    for kind in kinds:
+        with mcx.Engine([descs[q]]) as eng:
+            eng.pass_kind = kind
+            eng.init_random(0, 11 + q)
+            eng.sweep(n - 1)
+            before = eng.get_state(0)
+            st = eng.stats(0)
+            ang, sweep = float(st[mcx.ST_ANG_VAR]), int(st[mcx.ST_SWEEP_INDEX])
+            eng.sweep(1)
+            states[kind] = (before, ang, sweep, eng.get_state(0))
+    (b0, ang, sweep, sm), (b1, ang1, sweep1, sd) = states["march"], states["direct"]
+    assert np.array_equal(b0, b1) and ang == ang1 and sweep == sweep1 == n - 1
+    lat = O.Lattice(m)
+    i = np.arange(m.n) % m.nx
+    j = (np.arange(m.n) // m.nx) % m.ny
+    k = np.arange(m.n) // (m.nx * m.ny)
+    colour = (i + j + k) & 1
+    differ = np.nonzero(np.any(sm != sd, axis=1))[0]
+    assert len(differ) > 0
+    # colour 0 is updated first: a colour-0 site that differs saw identical
+    # neighbours; otherwise only colour-1 sites differ, and their colour-0
+    # neighbours agree after the sweep
+    c = 0 if np.any(colour[differ] == 0) else 1
+    lat.ni[:] = b0
+    if c == 1:
+        lat.ni[colour == 0] = sm[colour == 0]
+    flips = 0
+    for s in differ[colour[differ] == c]:
+        u = O.site_uniforms(m, int(s), 500 + q, q, sweep)
+        p64 = O.propose(b0[s], u[0], u[1], ang)
+        moved = [x for x in (sm[s], sd[s]) if not np.array_equal(x, b0[s])]
+        for x in moved:  # every accepted proposal is the oracle's, to FP32 rounding
+            assert np.max(np.abs(x - p64)) < 3e-6, (int(s), x, p64)
+        if len(moved) == 1:  # one form accepted, the other rejected: a near-tie
+            flips += 1
+            d64 = lat.local_energy(int(s), p64) - lat.local_energy(int(s), b0[s])
+            pa = np.exp(-d64 / T)
+            assert abs(u[2] - pa) <= TIE * (1 + pa), (int(s), u[2], pa, d64)
+    print(f"parted at sweep {n} in replica {q}: {len(differ)} sites differ, {flips} near-tie decisions of colour {c}")
