@@ -115,7 +115,7 @@ def run_c3(replicas=256, sweeps=50, steps=3, seed=3, pass_shape=None):
             "mean_S": float(S)}
 
 
-def run_c5(replicas=64, sweeps=20, proposal="plain", side=96, radius=40.0, train_samples=1_000_000):
+def run_c5(replicas=64, sweeps=20, proposal="plain", side=96, radius=40.0, train_samples=1_000_000, pass_shape=None):
     from . import gain
     descs = c5_descs(replicas, side, radius)
     sites = replicas * side ** 3
@@ -125,8 +125,8 @@ def run_c5(replicas=64, sweeps=20, proposal="plain", side=96, radius=40.0, train
     with Engine(descs) as eng:
         for q in range(replicas):
             eng.init_random(q, 11 + q)
-        tuned = eng.autotune()
-        out["pass_kernel"] = f"{eng.pass_kind} {tuned[0]} x {tuned[1]} (autotuned)"
+        tuned = _shape(eng, pass_shape)
+        out["pass_kernel"] = f"{eng.pass_kind} {tuned[0]} x {tuned[1]}" + ("" if pass_shape else " (autotuned)")
         eng.sweep(200)
         if proposal != "plain":
             eng.set_mlp(gain.init_weights(5))
@@ -154,12 +154,12 @@ def main():
     ap.add_argument("--sweeps", type=int, default=None)
     ap.add_argument("--proposal", default="plain", choices=["plain", "vmf_mlp"])
     ap.add_argument("--steps", type=int, default=3, help="c3: timed blocks")
-    ap.add_argument("--pass-shape", default=None, help="c3: KIND:BLOCK:PLANES instead of the autotuner's choice")
+    ap.add_argument("--pass-shape", default=None, help="KIND:BLOCK:PLANES instead of the autotuner's choice")
     a = ap.parse_args()
     if a.which == "c3":
         res = run_c3(replicas=a.replicas or 256, sweeps=a.sweeps or 50, steps=a.steps, pass_shape=a.pass_shape)
     else:
-        res = run_c5(replicas=a.replicas or 64, sweeps=a.sweeps or 20, proposal=a.proposal)
+        res = run_c5(replicas=a.replicas or 64, sweeps=a.sweeps or 20, proposal=a.proposal, pass_shape=a.pass_shape)
     print(json.dumps(res), flush=True)
 
 
