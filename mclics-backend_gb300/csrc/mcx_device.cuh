@@ -95,15 +95,12 @@ __host__ __device__ __forceinline__ uint32_t fastdiv(uint32_t n, uint32_t m, int
 // ---------------------------------------------------------------------------
 // Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11).
 // ---------------------------------------------------------------------------
+// One widening multiply gives both halves (on the GPU a single 32x32->64
+// multiply-add instead of separate low and high multiplies).
 __host__ __device__ __forceinline__ void mulhilo32(uint32_t a, uint32_t b, uint32_t &hi, uint32_t &lo) {
-#ifdef __CUDA_ARCH__
-  lo = a * b;
-  hi = __umulhi(a, b);
-#else
-  uint64_t p = (uint64_t)a * b;
+  const unsigned long long p = (unsigned long long)a * b;
   hi = (uint32_t)(p >> 32);
   lo = (uint32_t)p;
-#endif
 }
 
 __host__ __device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint32_t k0, uint32_t k1) {
