@@ -173,6 +173,9 @@ def _cpu_reference_worker(seconds, cores, q):
 
 def _cpu_reference(seconds, cores):
     import multiprocessing as mp
+    # the worker's OpenMP runtime reads this when the library loads (a
+    # launcher such as torchrun sets it to 1 for every rank)
+    os.environ["OMP_NUM_THREADS"] = str(cores)
     ctx = mp.get_context("spawn")
     q = ctx.Queue()
     p = ctx.Process(target=_cpu_reference_worker, args=(seconds, cores, q))
@@ -187,8 +190,8 @@ def _cpu_reference(seconds, cores):
 def _cpu_port(seconds, cores):
     from oracle import oracle as O
     m = O.Model(nx=NX, ny=NY, nz=NZ)
+    os.environ["OMP_NUM_THREADS"] = str(cores)  # before the oracle library's OpenMP runtime loads
     lat = O.Lattice(m)
-    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
     a = np.float32(0.5)
     lat.sweep(TI, a, 1, 0, 0, "eight", O.F_PARALLEL | O.F_NO_NORMALIZE)
     n, t0 = 0, time.perf_counter()
@@ -221,8 +224,8 @@ def run_reference(args, ws, rank):
                 times.append(SITES / r["value"] * 2)
         sample = 2
     else:
+        os.environ["OMP_NUM_THREADS"] = str(cores)  # before the oracle library's OpenMP runtime loads
         from oracle import oracle as O
-        os.environ.setdefault("OMP_NUM_THREADS", str(cores))
         lat = O.Lattice(O.Model(nx=NX, ny=NY, nz=NZ))
         a = np.float32(0.5)
         sweep = 0

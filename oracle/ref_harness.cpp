@@ -184,13 +184,21 @@ extern "C" float ref_local_energy(const float *field, long site, const float n[3
   return G->latice_Potential(loc);
 }
 
+/* Threads for a sweep: the request, but never more than the generators made
+ * at setup (one per thread that OpenMP offered then), since each sweep thread
+ * draws from its own. */
+static int sweep_threads(int nthreads) {
+  const int made = (int)RNG.size();
+  return nthreads > 0 && nthreads < made ? nthreads : made;
+}
+
 /* One EvolveN::Monte_Carlo_Step (src/evolve.cpp:64-179).  With feed != NULL
  * the sweep runs on one thread and draws its uniforms from feed in order;
  * returns the number of uniforms consumed. */
 extern "C" long ref_sweep(float *ni, float T, float *ang_var, const double *feed, long nfeed, int nthreads) {
   memcpy(NI, ni, sizeof(float) * 3 * NT);
   P->T = T;
-  omp_set_num_threads(feed ? 1 : (nthreads > 0 ? nthreads : (int)RNG.size()));
+  omp_set_num_threads(feed ? 1 : sweep_threads(nthreads));
   mcx_shim_feed(feed, nfeed);
   EV->Monte_Carlo_Step(*ang_var, RNG.data());
   long used = mcx_shim_feed_used();
@@ -204,7 +212,7 @@ extern "C" void ref_set_state(const float *ni) { memcpy(NI, ni, sizeof(float) * 
 extern "C" void ref_get_state(float *ni) { memcpy(ni, NI, sizeof(float) * 3 * NT); }
 extern "C" float ref_sweeps_inplace(int n, float T, float ang_var, int nthreads) {
   P->T = T;
-  omp_set_num_threads(nthreads > 0 ? nthreads : (int)RNG.size());
+  omp_set_num_threads(sweep_threads(nthreads));
   for (int s = 0; s < n; s++) EV->Monte_Carlo_Step(ang_var, RNG.data());
   return ang_var;
 }
