@@ -139,9 +139,10 @@ enum {
 
 int mcx_version(void);
 
-/* Allocates the device state for n_replicas replicas (each any size with even
- * nx; periodic y/z need even ny/nz) and fills the geometry masks of
- * bulk/slab/sphere replicas.  Directors start along +z; use mcx_set_state or
+/* Allocates the device state for n_replicas replicas (any sizes; an axis that
+ * is periodic after the geometry forces the bounds must have even length, as
+ * red/black sweeps need -- MCX_ERR_UNSUPPORTED otherwise) and fills the
+ * geometry masks of bulk/slab/sphere replicas.  Directors start along +z; use mcx_set_state or
  * mcx_init_random / mcx_init_homogeneous to set them. */
 mcx_status mcx_create(int n_replicas, const mcx_replica_desc *descs, mcx_engine **out);
 void mcx_destroy(mcx_engine *eng);

@@ -222,7 +222,6 @@ extern "C" void mcx_destroy(mcx_engine *e) { free_engine(e); }
 static mcx_status check_desc(const mcx_replica_desc &d, int r) {
   if (d.nx < 2 || d.ny < 1 || d.nz < 1) return fail(nullptr, MCX_ERR_INVALID, "replica %d: lattice %dx%dx%d too small", r, d.nx, d.ny, d.nz);
   if ((long long)d.nx * d.ny * d.nz >= (1LL << 31)) return fail(nullptr, MCX_ERR_INVALID, "replica %d: more than 2^31 sites", r);
-  if (d.nx % 2) return fail(nullptr, MCX_ERR_UNSUPPORTED, "replica %d: nx = %d must be even (red/black rows)", r, d.nx);
   if (d.geometry < 0 || d.geometry > 3) return fail(nullptr, MCX_ERR_INVALID, "replica %d: bad geometry %d", r, d.geometry);
   if (d.potential < 0 || d.potential > 2) return fail(nullptr, MCX_ERR_INVALID, "replica %d: bad potential %d", r, d.potential);
   if (d.n_surfaces < 0 || d.n_surfaces > MCX_MAX_SURFACES) return fail(nullptr, MCX_ERR_INVALID, "replica %d: bad surface count %d", r, d.n_surfaces);
@@ -234,8 +233,10 @@ static mcx_status check_desc(const mcx_replica_desc &d, int r) {
 }
 
 // Bounds as the geometry forces them (src/geometry_slab.cpp:23,
-// src/geometry_sphere.cpp:19-21), then the red/black requirement: a periodic
-// axis of odd length would make a site its own-colour neighbour.
+// src/geometry_sphere.cpp:19-21).  A periodic axis of odd length would make a
+// site its own-colour neighbour, so red/black sweeps need even lengths on
+// periodic axes; free axes may have any length (an odd nx is stored padded:
+// odd_tail in mcx_pass.cuh).
 static void effective_bounds(mcx_replica_desc &d) {
   if (d.geometry == MCX_GEO_SLAB) d.zbound = MCX_BOUND_FREE;
   if (d.geometry == MCX_GEO_SPHERE) d.xbound = d.ybound = d.zbound = MCX_BOUND_FREE;
@@ -352,8 +353,12 @@ extern "C" mcx_status mcx_create(int n, const mcx_replica_desc *descs, mcx_engin
       return fail(nullptr, MCX_ERR_UNSUPPORTED, "all replicas of one engine must use the same pair potential");
     mcx_replica_desc d = descs[r];
     effective_bounds(d);
-    if ((d.ybound == MCX_BOUND_PERIODIC && d.ny % 2) || (d.zbound == MCX_BOUND_PERIODIC && d.nz % 2))
-      return fail(nullptr, MCX_ERR_UNSUPPORTED, "replica %d: periodic y/z axes need even ny/nz for red/black sweeps", r);
+    if ((d.xbound == MCX_BOUND_PERIODIC && d.nx % 2) || (d.ybound == MCX_BOUND_PERIODIC && d.ny % 2) ||
+        (d.zbound == MCX_BOUND_PERIODIC && d.nz % 2))
+      return fail(nullptr, MCX_ERR_UNSUPPORTED,
+                  "replica %d: lattice %dx%dx%d has an odd periodic axis; red/black sweeps need even lengths on "
+                  "periodic axes (odd lengths are supported on free axes)",
+                  r, d.nx, d.ny, d.nz);
   }
   mcx_engine *e = new mcx_engine();
   e->nrep = n;
@@ -373,7 +378,7 @@ extern "C" mcx_status mcx_create(int n, const mcx_replica_desc *descs, mcx_engin
     R.nx = d.nx;
     R.ny = d.ny;
     R.nz = d.nz;
-    R.hx = d.nx / 2;
+    R.hx = (d.nx + 1) / 2;  // odd nx: one padding slot per row (odd_tail)
     R.hs = (int)align_up(R.hx, 4);
     R.xb = d.xbound;
     R.yb = d.ybound;
@@ -421,7 +426,8 @@ extern "C" mcx_status mcx_create(int n, const mcx_replica_desc *descs, mcx_engin
       R.dy[s] = ax[1];
       R.dz[s] = ax[2];
     }
-    if (d.geometry != MCX_GEO_BULK) e->var.mask = true;
+    // an odd nx needs the mask: its padding slots are inactive sites
+    if (d.geometry != MCX_GEO_BULK || d.nx % 2) e->var.mask = true;
     if (d.xbound != MCX_BOUND_PERIODIC || d.ybound != MCX_BOUND_PERIODIC || d.zbound != MCX_BOUND_PERIODIC ||
         d.nx % 4 != 0)
       e->var.per = false;
@@ -448,6 +454,9 @@ extern "C" mcx_status mcx_create(int n, const mcx_replica_desc *descs, mcx_engin
     const char *kb = getenv("MCX_STAGE_KB");
     const long long budget = (kb ? atoll(kb) : 40) * 1024;
     e->can_stage = true;
+    // the staged pass does not handle the padding slots of an odd nx
+    for (int r = 0; r < n; r++)
+      if (e->rep[r].nx % 2) e->can_stage = false;
     for (int r = 0; r < n && e->can_stage; r++) {
       RepDev &R = e->rep[r];
       if (!plan_tiles(R, e->var.mask, budget)) {
@@ -667,7 +676,8 @@ extern "C" mcx_status mcx_set_mask(mcx_engine *e, int r, const int *pt, const fl
       any |= pt[row * R.nx + i] != 0;
       bulk &= pt[row * R.nx + i] == 1;
     }
-    act[row] = bulk ? 1 : (any ? 2 : 0);
+    // an odd-nx row also holds a padding slot (inactive): never a bulk row
+    act[row] = bulk && R.nx % 2 == 0 ? 1 : (any ? 2 : 0);
   }
   mark_dead_units(e);
   if (e->d_units && !e->units.empty())

@@ -107,6 +107,9 @@ __global__ void __launch_bounds__(kLPB, MCX_LMARCH_MIN_BLOCKS) k_lmarch(PassArgs
       nbA[1][0] = exv[0]; nbA[1][1] = exv[1]; nbA[1][2] = exv[2]; eA[1] = exe; wA[1] = wt(exe, pex);
       nbB[0][0] = o0.v[0].y; nbB[0][1] = o0.v[1].y; nbB[0][2] = o0.v[2].y; eB[0] = 1.f; wB[0] = wt(1.f, hi);
       nbB[1][0] = o0.v[0].x; nbB[1][1] = o0.v[1].x; nbB[1][2] = o0.v[2].x; eB[1] = 1.f; wB[1] = wt(1.f, lo);
+      // odd nx: the row's last site has no x+ bond (odd_tail, mcx_pass.cuh)
+      if (MASK && m.tail == 1) eA[0] = wA[0] = 0.f;
+      if (MASK && m.tail == 2) eB[0] = wB[0] = 0.f;
     } else {
       if (m.hasB) {
         nbA[0][0] = o0.v[0].y; nbA[0][1] = o0.v[1].y; nbA[0][2] = o0.v[2].y; eA[0] = 1.f; wA[0] = wt(1.f, hi);
@@ -141,7 +144,9 @@ __global__ void __launch_bounds__(kLPB, MCX_LMARCH_MIN_BLOCKS) k_lmarch(PassArgs
         yA[q] = Y[(2 * lane) * 4 + q];
         yB[q] = Y[(2 * lane + 1) * 4 + q];
       }
-      {
+      // odd nx: the phantom in the last slot of an s = 1 row is skipped
+      const bool skipA = MASK && s == 1 && m.tail == 1, skipB = MASK && s == 1 && m.tail == 2;
+      if (!skipA) {
         float sx = 0.f, sy = 0.f, sz = 0.f;
         if (MASK && psA > 1) {
           const float *nsb = a.ns + R.ns_off + (long long)(c * 3) * R.plane + m.off;
@@ -153,7 +158,7 @@ __global__ void __launch_bounds__(kLPB, MCX_LMARCH_MIN_BLOCKS) k_lmarch(PassArgs
         acc += site_update_learned<POT, MASK, FIELD, MODE>(R, a, c, ax.x, ay.x, az.x, nbA, wA, eA, psA, sx, sy, sz,
                                                            yA, invT, nat, sw, qs);
       }
-      if (m.hasB) {
+      if (m.hasB && !skipB) {
         float sx = 0.f, sy = 0.f, sz = 0.f;
         if (MASK && psB > 1) {
           const float *nsb = a.ns + R.ns_off + (long long)(c * 3) * R.plane + m.off + 1;

@@ -57,7 +57,7 @@ __device__ __forceinline__ void march_plane(const PassArgs &a, const RepDev &R, 
   }
   update_pair<POT, MASK, FIELD, MODE, PER>(a, R, c, m.s, m.hasB, m.ee0, m.ee1, m.eyp, m.eym, o0, yp, ym, op, om, exv,
                                            pself, pex, zp, zm, m.pid, m.off, seed, stream, sw, ang, invT, ax, ay, az,
-                                           acc, qs);
+                                           acc, qs, m.tail);
   *reinterpret_cast<float2 *>(m.A0 + m.off) = ax;
   *reinterpret_cast<float2 *>(m.A1 + m.off) = ay;
   *reinterpret_cast<float2 *>(m.A2 + m.off) = az;

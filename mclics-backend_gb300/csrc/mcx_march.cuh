@@ -45,6 +45,7 @@ struct March {
   int s;                            // parity of the own sites in this plane
   int h0, row;                      // half-row index of site A; row j + ny * k of this plane
   bool hasB;
+  uint8_t tail;                     // odd nx: 1 / 2 when site A / B sits in the row's last slot (0 otherwise)
   float ee0, ee1, eyp, eym;         // bond present: extra x (s = 0, 1), y+1, y-1
 };
 
@@ -62,17 +63,21 @@ __device__ __forceinline__ void grid_dependency_wait(March &m) {
 // A dead unit (kUnitDead) of a masked lattice: in measured sweeps with a
 // field, each own (inactive) site adds its field energy, in the order the
 // full update adds it; nothing else.
+// The slot of a phantom site (odd nx, a row whose own sites are odd) is
+// skipped.
 template <bool FIELD, int MODE>
 __device__ __forceinline__ void dead_unit(const RepDev &R, March &m, int kb, int ke, float qs[kQ]) {
   if (!(FIELD && MODE == MODE_SWEEP_MEASURE)) return;
+  int s = m.s;
 #pragma unroll 1
   for (int k = kb; k < ke; k++) {
     const float2 x = *reinterpret_cast<const float2 *>(m.A0 + m.off);
     const float2 y = *reinterpret_cast<const float2 *>(m.A1 + m.off);
     const float2 z = *reinterpret_cast<const float2 *>(m.A2 + m.off);
-    qs[0] += field_energy(R, x.x, y.x, z.x);
-    if (m.hasB) qs[0] += field_energy(R, x.y, y.y, z.y);
+    if (!(s && m.tail == 1)) qs[0] += field_energy(R, x.x, y.x, z.x);
+    if (m.hasB && !(s && m.tail == 2)) qs[0] += field_energy(R, x.y, y.y, z.y);
     m.off += m.dz;
+    s ^= 1;
   }
 }
 
@@ -98,6 +103,7 @@ __device__ __forceinline__ void march_init(const PassArgs &a, const RepDev &R, i
     const int j = (int)fastdiv((uint32_t)p, R.hp_m, R.hp_p);
     const int h0 = 2 * (p - j * R.hp);
     m.hasB = h0 + 1 < hx;
+    m.tail = odd_tail<MASK>(R, h0);
     // the x neighbour outside the opposite pair: x- of A when s = 0, x+ of B
     // (or of A when the pair has no B) when s = 1
     int ex0 = h0 - 1, ex1 = m.hasB ? h0 + 2 : h0 + 1;
@@ -165,7 +171,8 @@ __device__ __forceinline__ void update_pair_draw(const PassArgs &a, const RepDev
                                                  const OPair &yp, const OPair &ym, const OPair &op, const OPair &om,
                                                  const float exv[3], uint16_t pself, uint8_t pex, bool zp, bool zm,
                                                  const uint4 rw, long long ns_at, float ang, float invT, float2 &ax,
-                                                 float2 &ay, float2 &az, unsigned &acc, float qs[kQ]) {
+                                                 float2 &ay, float2 &az, unsigned &acc, float qs[kQ],
+                                                 int tail = 0) {
   float uA[3], uB[3];
   pair_uniforms(rw, uA, uB);
   auto wt = [&](float ee, uint8_t pp) { return MASK ? (ee != 0.f && pp != 0 ? 1.f : 0.f) : ee; };
@@ -177,7 +184,10 @@ __device__ __forceinline__ void update_pair_draw(const PassArgs &a, const RepDev
   const uint8_t lo = (uint8_t)(o0.pt & 0xFF), hi = (uint8_t)(o0.pt >> 8);
   const int P = R.plane;
   float nb[6][3], w[6], e[6];
-  {  // site A
+  // odd nx (masked only): a phantom in the last slot of an s = 1 row is
+  // skipped; the last site of an s = 0 row has no x+ bond
+  const bool skipA = MASK && s == 1 && tail == 1, skipB = MASK && s == 1 && tail == 2;
+  if (!skipA) {  // site A
     if (s == 0) {
       nb[0][0] = o0.v[0].x; nb[0][1] = o0.v[1].x; nb[0][2] = o0.v[2].x; e[0] = 1.f; w[0] = wt(1.f, lo);
       nb[1][0] = exv[0]; nb[1][1] = exv[1]; nb[1][2] = exv[2]; e[1] = exe; w[1] = wt(exe, pex);
@@ -189,6 +199,7 @@ __device__ __forceinline__ void update_pair_draw(const PassArgs &a, const RepDev
       }
       nb[1][0] = o0.v[0].x; nb[1][1] = o0.v[1].x; nb[1][2] = o0.v[2].x; e[1] = 1.f; w[1] = wt(1.f, lo);
     }
+    if (MASK && s == 0 && tail == 1) e[0] = w[0] = 0.f;
 #pragma unroll
     for (int q = 0; q < 4; q++) {
       const OPair &o = *rows4[q];
@@ -207,10 +218,11 @@ __device__ __forceinline__ void update_pair_draw(const PassArgs &a, const RepDev
     acc += site_update<POT, MASK, FIELD, MODE>(R, a, c, ax.x, ay.x, az.x, nb, w, e, ps, sx, sy, sz, uA, ang, invT,
                                                0u, qs);
   }
-  if (hasB) {  // site B
+  if (hasB && !skipB) {  // site B
     if (s == 0) {
       nb[0][0] = o0.v[0].y; nb[0][1] = o0.v[1].y; nb[0][2] = o0.v[2].y; e[0] = 1.f; w[0] = wt(1.f, hi);
       nb[1][0] = o0.v[0].x; nb[1][1] = o0.v[1].x; nb[1][2] = o0.v[2].x; e[1] = 1.f; w[1] = wt(1.f, lo);
+      if (MASK && tail == 2) e[0] = w[0] = 0.f;
     } else {
       nb[0][0] = exv[0]; nb[0][1] = exv[1]; nb[0][2] = exv[2]; e[0] = exe; w[0] = wt(exe, pex);
       nb[1][0] = o0.v[0].y; nb[1][1] = o0.v[1].y; nb[1][2] = o0.v[2].y; e[1] = 1.f; w[1] = wt(1.f, hi);
@@ -248,10 +260,10 @@ __device__ __forceinline__ void update_pair(const PassArgs &a, const RepDev &R, 
                                             uint16_t pself, uint8_t pex, bool zp, bool zm, uint32_t pid,
                                             long long ns_at, uint32_t seed, uint32_t stream, unsigned long long sw,
                                             float ang, float invT, float2 &ax, float2 &ay, float2 &az, unsigned &acc,
-                                            float qs[kQ]) {
+                                            float qs[kQ], int tail = 0) {
   update_pair_draw<POT, MASK, FIELD, MODE, PER>(a, R, c, s, hasB_, ee0, ee1, eyp, eym, o0, yp, ym, op, om, exv, pself,
                                                 pex, zp, zm, pair_draw(pid, c, sw, seed, stream), ns_at, ang, invT, ax,
-                                                ay, az, acc, qs);
+                                                ay, az, acc, qs, tail);
 }
 
 }  // namespace mcx

@@ -327,10 +327,24 @@ struct PairStage {
   uint32_t pw[MASK ? 7 : 1][kPB];  // point-type words: own, other row, 4 rows, extra
 };
 
+// Odd nx (free x bound only): a colour's sites of a row are i = 2h + s
+// (s = (c + j + k) & 1), h < hx = (nx + 1) / 2, so the row's last storage
+// slot h = hx - 1 holds the real site nx - 1 when s = 0 -- its x+ slot is the
+// other colour's phantom, so it has no x+ bond -- and a phantom (i = nx) when
+// s = 1.  Phantoms have point type 0, never move and add nothing to a
+// measurement.  Returns 1 / 2 when site A / B of the pair at h0 is in that
+// slot, else 0 (always 0 in unmasked kernels: an odd-nx replica has a mask).
+template <bool MASK>
+__device__ __forceinline__ uint8_t odd_tail(const RepDev &R, int h0) {
+  if (!MASK || !(R.nx & 1)) return 0;
+  return h0 == R.hx - 1 ? 1 : (h0 + 1 == R.hx - 1 ? 2 : 0);
+}
+
 // Where a thread's pair lives and who its neighbours are.
 struct PairGeom {
   int row, h0, j, k, s, off, exh, offp;
   bool valid, hasB;
+  uint8_t tail;  // odd_tail
   float exe, er[4];
   int rr[4];
 };
@@ -344,6 +358,7 @@ __device__ __forceinline__ void pair_geom(const RepDev &R, int c, int t, PairGeo
   g.j = g.row - g.k * R.ny;
   g.s = (c + g.j + g.k) & 1;
   g.hasB = g.h0 + 1 < R.hx;
+  g.tail = odd_tail<true>(R, g.h0);
   g.off = g.row * R.hs + g.h0;
   g.offp = g.row * R.hps + g.h0;
   g.exe = 1.f;
@@ -435,10 +450,14 @@ __device__ __forceinline__ void compute_pair(const PassArgs &a, int c, int2 m, c
   }
   auto wt = [&](float ee, uint8_t pp) { return MASK ? (ee != 0.f && pp != 0 ? 1.f : 0.f) : ee; };
   float nb[6][3], w[6], e[6];
-  {
+  // odd nx: the phantom of an s = 1 row is skipped, the last site of an
+  // s = 0 row has no x+ bond (odd_tail)
+  const bool skipA = MASK && g.s == 1 && g.tail == 1, skipB = MASK && g.s == 1 && g.tail == 2;
+  if (!skipA) {
     if (g.s == 0) {
       nb[0][0] = ox.x; nb[0][1] = oy.x; nb[0][2] = oz.x; e[0] = 1.f; w[0] = wt(1.f, po2.x);
       nb[1][0] = ex; nb[1][1] = ey; nb[1][2] = ez; e[1] = g.exe; w[1] = wt(g.exe, pex);
+      if (MASK && g.tail == 1) e[0] = w[0] = 0.f;
     } else {
       if (g.hasB) {
         nb[0][0] = ox.y; nb[0][1] = oy.y; nb[0][2] = oz.y; e[0] = 1.f; w[0] = wt(1.f, po2.y);
@@ -466,10 +485,11 @@ __device__ __forceinline__ void compute_pair(const PassArgs &a, int c, int2 m, c
     acc += site_update<POT, MASK, FIELD, MODE>(R, a, c, ax.x, ay.x, az.x, nb, w, e, ps, sx, sy, sz, uA, ang, invT,
                                                nat, qs);
   }
-  if (g.hasB) {
+  if (g.hasB && !skipB) {
     if (g.s == 0) {
       nb[0][0] = ox.y; nb[0][1] = oy.y; nb[0][2] = oz.y; e[0] = 1.f; w[0] = wt(1.f, po2.y);
       nb[1][0] = ox.x; nb[1][1] = oy.x; nb[1][2] = oz.x; e[1] = 1.f; w[1] = wt(1.f, po2.x);
+      if (MASK && g.tail == 2) e[0] = w[0] = 0.f;
     } else {
       nb[0][0] = ex; nb[0][1] = ey; nb[0][2] = ez; e[0] = g.exe; w[0] = wt(g.exe, pex);
       nb[1][0] = ox.y; nb[1][1] = oy.y; nb[1][2] = oz.y; e[1] = 1.f; w[1] = wt(1.f, po2.y);
@@ -645,6 +665,8 @@ __device__ __forceinline__ void compute_pair_learned(const PassArgs &a, int c, i
     nbA[1][0] = ex; nbA[1][1] = ey; nbA[1][2] = ez; eA[1] = g.exe; wA[1] = wt(g.exe, pex);
     nbB[0][0] = ox.y; nbB[0][1] = oy.y; nbB[0][2] = oz.y; eB[0] = 1.f; wB[0] = wt(1.f, po2.y);
     nbB[1][0] = ox.x; nbB[1][1] = oy.x; nbB[1][2] = oz.x; eB[1] = 1.f; wB[1] = wt(1.f, po2.x);
+    if (MASK && g.tail == 1) eA[0] = wA[0] = 0.f;
+    if (MASK && g.tail == 2) eB[0] = wB[0] = 0.f;
   } else {
     if (g.hasB) {
       nbA[0][0] = ox.y; nbA[0][1] = oy.y; nbA[0][2] = oz.y; eA[0] = 1.f; wA[0] = wt(1.f, po2.y);
@@ -682,7 +704,8 @@ __device__ __forceinline__ void compute_pair_learned(const PassArgs &a, int c, i
   float2 ax = st.v[0][tid], ay = st.v[1][tid], az = st.v[2][tid];
   const unsigned long long sw = UPD ? S->sweep : 0ull;
   const float invT = UPD ? 1.0f / S->T : 0.f;
-  {
+  const bool skipA = MASK && g.s == 1 && g.tail == 1, skipB = MASK && g.s == 1 && g.tail == 2;
+  if (!skipA) {
     float sx = 0.f, sy = 0.f, sz = 0.f;
     if (MASK && psA > 1) {
       const float *nsb = a.ns + R.ns_off + (long long)(c * 3) * P + g.off;
@@ -694,7 +717,7 @@ __device__ __forceinline__ void compute_pair_learned(const PassArgs &a, int c, i
     acc += site_update_learned<POT, MASK, FIELD, MODE>(R, a, c, ax.x, ay.x, az.x, nbA, wA, eA, psA, sx, sy, sz, yA,
                                                        invT, nat, sw, qs);
   }
-  if (g.hasB) {
+  if (g.hasB && !skipB) {
     float sx = 0.f, sy = 0.f, sz = 0.f;
     if (MASK && psB > 1) {
       const float *nsb = a.ns + R.ns_off + (long long)(c * 3) * P + g.off + 1;

@@ -209,9 +209,22 @@ mcx_status prepare(const char *path, SimParams &P, mcx_replica_desc &d, std::vec
     g_err = "evol mode '" + P.evol + "' not implemented. Options: thermal | step | quench | electric (GPU / GB300 suffix accepted)";
     return MCX_ERR_PARSE;
   }
-  if (d.nx % 2) {
-    g_err = "Nx = " + std::to_string(d.nx) + " must be even for red/black sweeps";
-    return MCX_ERR_UNSUPPORTED;
+  {
+    // bounds as the geometry forces them (src/geometry_slab.cpp:23,
+    // src/geometry_sphere.cpp:19-21); red/black sweeps need even lengths on
+    // periodic axes, free axes may have any length
+    const bool sph = d.geometry == MCX_GEO_SPHERE;
+    const int xb = sph ? MCX_BOUND_FREE : d.xbound, yb = sph ? MCX_BOUND_FREE : d.ybound;
+    const int zb = sph || d.geometry == MCX_GEO_SLAB ? MCX_BOUND_FREE : d.zbound;
+    const char *ax = (xb == MCX_BOUND_PERIODIC && d.nx % 2) ? "Nx"
+                     : (yb == MCX_BOUND_PERIODIC && d.ny % 2) ? "Ny"
+                     : (zb == MCX_BOUND_PERIODIC && d.nz % 2) ? "Nz"
+                                                              : nullptr;
+    if (ax) {
+      g_err = std::string(ax) + " is odd on a periodic axis (" + std::to_string(d.nx) + "x" + std::to_string(d.ny) +
+              "x" + std::to_string(d.nz) + "); red/black sweeps need even lengths on periodic axes";
+      return MCX_ERR_UNSUPPORTED;
+    }
   }
   if (im == 0 && P.dT == 0) {
     g_err = "dT must be non-zero";

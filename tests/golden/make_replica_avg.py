@@ -21,7 +21,8 @@ import tempfile
 
 import numpy as np
 
-REF = "/root/reference"
+# the McLiCS source tree whose average_replicas.py this script runs
+REF = os.environ.get("MCLICS_REFERENCE_TREE", "/root/reference")
 OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "replica_avg.json")
 
 

@@ -73,6 +73,36 @@ def _check(path):
     return st, d, mcx.lib().mcx_last_error(None).decode()
 
 
+def _samples():
+    import json
+    with open(os.path.join(ROOT, "tests", "golden", "reference_samples.json")) as f:
+        return json.load(f)
+
+
+@pytest.mark.parametrize("name", sorted(_samples()))
+def test_every_reference_sample_file_is_accepted(name, tmp_path):
+    """The reference's eight sample parameter files (key/value lines kept by
+    tests/golden/make_sample_params.py) parse and validate, including the
+    odd-sided droplets of test4.txt (25^3) and input_parameters.txt (61^3)."""
+    text = _samples()[name]
+    p = tmp_path / name
+    p.write_text(text)
+    st, d, err = _check(p)
+    assert st == 0, err
+    kv = {ln.split()[0].lower(): ln.split()[1] for ln in text.splitlines()}
+    assert (d.nx, d.ny, d.nz) == (int(kv["nx"]), int(kv["ny"]), int(kv["nz"]))
+
+
+def test_odd_periodic_axis_is_refused_with_a_reason(tmp_path):
+    p = tmp_path / "p.txt"
+    p.write_text("Nx 15\nNy 16\nNz 16\nxbound periodic\n")
+    st, d, err = _check(p)
+    assert st == 4 and "odd" in err and "periodic" in err
+    p.write_text("Nx 15\nNy 16\nNz 16\nxbound free\n")
+    st, d, err = _check(p)
+    assert st == 0, err
+
+
 def test_parser_reads_reference_sample_style(tmp_path):
     p = tmp_path / "p.txt"
     p.write_text(textwrap.dedent("""\
@@ -120,7 +150,7 @@ def test_parser_reads_reference_sample_style(tmp_path):
     ("geometry sphere\nanchoring_type 0 nonsense\nW 0 1\n", 6, "not defined"),
     ("geometry sphere\nanchoring_type 0 rp\nW 0 1\n", 6, "phi_s"),
     ("potential gay_berne\n", 6, "ll | ghrl | pear"),
-    ("Nx 15\n", 4, "even"),
+    ("Nx 15\nxbound periodic\n", 4, "even lengths on periodic axes"),
     ("evol sideways\n", 6, "evol mode"),
     ("dT 0\n", 6, "dT"),
 ])
