@@ -58,6 +58,21 @@ def _setup(L, m: dict):
         L.ref_set_pear(f(m["B1"]), f(m["C"]))
 
 
+def _active(L, n: int) -> np.ndarray:
+    pt = np.zeros(n, np.int32)
+    ns = np.zeros((n, 3), np.float32)
+    L.ref_get_mask(_p(pt), _p(ns))
+    return pt != 0
+
+
+def _length_drift(ni: np.ndarray, act: np.ndarray) -> float:
+    """Mean of |n|^2 - 1 over the active sites: the reference's CPU sweep
+    does not renormalise its proposals (src/evolve.cpp:139-151), so director
+    lengths drift by float rounding, and E and S with them."""
+    v = ni.reshape(-1, 3)[act].astype(np.float64)
+    return float(np.mean(np.sum(v * v, axis=1) - 1.0))
+
+
 def _worker(m: dict, ops: List[tuple]) -> List[Any]:
     devnull = os.open(os.devnull, os.O_WRONLY)
     os.dup2(devnull, 1)  # the reference prints its setup banner to stdout
@@ -117,6 +132,7 @@ def _worker(m: dict, ops: List[tuple]) -> List[Any]:
             rows = []
             Q = np.zeros(9, np.float32)
             v = np.zeros(3, np.float32)
+            act = _active(L, n)
             for T in temps:
                 for _ in range(mct):
                     L.ref_sweep(_p(ni), C.c_float(T), C.byref(a), None, 0, nth)
@@ -125,7 +141,7 @@ def _worker(m: dict, ops: List[tuple]) -> List[Any]:
                     L.ref_sweep(_p(ni), C.c_float(T), C.byref(a), None, 0, nth)
                     E1 += float(L.ref_energy(_p(ni)))
                     S1 += float(L.ref_order(_p(ni), _p(Q), _p(v)))
-                rows.append((T, S1 / mcs, E1 / mcs))
+                rows.append((T, S1 / mcs, E1 / mcs, _length_drift(ni, act)))
             out.append(np.array(rows))
         elif kind == "field_sweep":
             # electricEvolveN::run (src/evolve_electric.cpp:28-90): at T = Ti, per
@@ -140,6 +156,7 @@ def _worker(m: dict, ops: List[tuple]) -> List[Any]:
             rows = []
             Q = np.zeros(9, np.float32)
             v = np.zeros(3, np.float32)
+            act = _active(L, n)
             for Ef in fields:
                 L.ref_set_field(C.c_float(Ef))
                 for _ in range(mct):
@@ -149,7 +166,7 @@ def _worker(m: dict, ops: List[tuple]) -> List[Any]:
                     L.ref_sweep(_p(ni), C.c_float(T), C.byref(a), None, 0, nth)
                     E1 += float(L.ref_energy(_p(ni)))
                     S1 += float(L.ref_order(_p(ni), _p(Q), _p(v)))
-                rows.append((Ef, S1 / mcs, E1 / mcs))
+                rows.append((Ef, S1 / mcs, E1 / mcs, _length_drift(ni, act)))
             out.append(np.array(rows))
         elif kind == "order":
             ni = np.ascontiguousarray(op[1], np.float32)

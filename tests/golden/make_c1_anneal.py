@@ -65,13 +65,15 @@ def main():
     with ctx.Pool(min(RUNS, os.cpu_count() or 1), maxtasksperchild=1) as pool:
         runs = pool.map(one_run, range(1, RUNS + 1))
     arr = np.array(runs)  # [run, T, (T, S, E)]
-    S, E = arr[:, :, 1], arr[:, :, 2]
+    S, E, D = arr[:, :, 1], arr[:, :, 2], arr[:, :, 3]
     out = {
         "config": "LL bulk 16^3 periodic, A=1, random ic, Ti=1.2 Tf=0.0 dT=-0.02, MCT=MCS=100 "
                   "(thermalEvolveN::run on the reference's CPU path)",
         "runs": RUNS, "temps": temps,
         "S_mean": S.mean(0).tolist(), "S_sem": (S.std(0, ddof=1) / np.sqrt(RUNS)).tolist(),
         "E_mean": E.mean(0).tolist(), "E_sem": (E.std(0, ddof=1) / np.sqrt(RUNS)).tolist(),
+        # the reference's director-length drift (mean |n|^2 - 1 over active sites)
+        "len2_drift_mean": D.mean(0).tolist(), "len2_drift_absmax": np.abs(D).max(0).tolist(),
     }
     with open(OUT, "w") as f:
         json.dump(out, f, indent=1)

@@ -116,12 +116,14 @@ def main():
         with ctx.Pool(min(RUNS, os.cpu_count() or 1), maxtasksperchild=1) as pool:
             runs = pool.map(one_run, [(name, s) for s in range(1, RUNS + 1)])
         arr = np.array(runs)  # [run, step, (T or field, S, E)]
-        S, E = arr[:, :, 1], arr[:, :, 2]
+        S, E, D = arr[:, :, 1], arr[:, :, 2], arr[:, :, 3]
         out = {
             "config": name, "model": c["model"], "mct": MCT, "mcs": MCS, "runs": RUNS,
             **({"T": c["T"], "fields": temps} if "T" in c else {"temps": temps}),
             "S_mean": S.mean(0).tolist(), "S_sem": (S.std(0, ddof=1) / np.sqrt(RUNS)).tolist(),
             "E_mean": E.mean(0).tolist(), "E_sem": (E.std(0, ddof=1) / np.sqrt(RUNS)).tolist(),
+            # the reference's director-length drift (mean |n|^2 - 1 over active sites)
+            "len2_drift_mean": D.mean(0).tolist(), "len2_drift_absmax": np.abs(D).max(0).tolist(),
         }
         path = os.path.join(HERE, name + ".json")
         with open(path, "w") as f:

@@ -41,3 +41,27 @@ def neighbours(lat, m, s):
             continue
         out[d] = lat.ni[t]
     return out
+
+
+def stat_parity_failures(G: np.ndarray, g: dict, key: str):
+    """Rows where the mean over runs of G (runs x rows) and the golden's mean
+    g[key + "_mean"] differ by more than 3 combined standard errors plus the
+    systematic of the reference's unrenormalised directors.
+
+    The reference's CPU sweep does not renormalise its proposals
+    (src/evolve.cpp:139-151), so its director lengths drift by float rounding;
+    the golden files record the drift measured in the reference's own runs
+    (len2_drift_absmax, the largest |mean |n|^2 - 1| over runs, per row; about
+    1e-7).  With |n|^2 = 1 + eps the order parameter moves by at most
+    1.5 eps and each bond or site energy term of degree <= 4 in the directors by
+    at most 2 eps of its size, so the allowance is 2 eps for S and
+    4 eps (|E| + 1) for E: below 1e-5 in every golden."""
+    R = G.shape[0]
+    m, se = G.mean(0), G.std(0, ddof=1) / np.sqrt(R)
+    rm, rse = np.asarray(g[key + "_mean"]), np.asarray(g[key + "_sem"])
+    sig = np.hypot(se, rse)
+    eps = np.asarray(g.get("len2_drift_absmax", np.zeros_like(rm)))
+    sysm = 2 * eps if key == "S" else 4 * eps * (np.abs(rm) + 1)
+    dev = np.abs(m - rm)
+    return [(int(i), float(m[i]), float(rm[i]), float(sig[i]), float(dev[i] / sig[i]))
+            for i in np.nonzero(dev > 3 * sig + sysm)[0]]

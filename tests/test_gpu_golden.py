@@ -11,9 +11,10 @@ E / S measurement, step size carried across temperatures.
 
 The chains differ (2-colour vs 8-colour order, Philox vs ranlxs0, renormalised
 vs unrenormalised proposals), so the comparison is statistical: at every T the
-means agree within 4 combined standard errors plus a small absolute allowance
-(1e-3 in S, 2e-3 in E, covering the reference's unrenormalised directors),
-and chi^2 per temperature over the whole curve stays below 2."""
+means agree within 3 combined standard errors (plus the systematic of the
+reference's director-length drift, measured in its runs and below 1e-5:
+helpers.stat_parity_failures), and chi^2 per temperature over the whole curve
+stays below 2."""
 import json
 import os
 
@@ -21,6 +22,7 @@ import numpy as np
 import pytest
 
 import mcx
+from helpers import stat_parity_failures
 
 pytestmark = pytest.mark.gpu
 
@@ -48,15 +50,12 @@ def test_c1_anneal_matches_reference_curves():
                 S[r, t] = st[mcx.ST_S1] / st[mcx.ST_N]
                 E[r, t] = st[mcx.ST_E1] / st[mcx.ST_N]
     chi2 = []
-    for name, G, tol in (("S", S, 1e-3), ("E", E, 2e-3)):
+    for name, G in (("S", S), ("E", E)):
+        bad = stat_parity_failures(G, g, name)
+        assert not bad, [(temps[i], *rest) for i, *rest in bad]
         m, se = G.mean(0), G.std(0, ddof=1) / np.sqrt(R)
-        rm, rse = np.array(g[name + "_mean"]), np.array(g[name + "_sem"])
-        sig = np.hypot(se, rse)
-        d = np.abs(m - rm)
-        bad = np.nonzero(d > 4 * sig + tol)[0]
-        assert len(bad) == 0, [(temps[i], m[i], rm[i], sig[i]) for i in bad]
-        z = d / np.maximum(sig, tol / 4)
-        chi2.append(float(np.mean(z ** 2)))
+        sig = np.hypot(se, np.array(g[name + "_sem"]))
+        chi2.append(float(np.mean(((m - np.array(g[name + "_mean"])) / sig) ** 2)))
     assert max(chi2) < 2.0, chi2
 
 
@@ -72,9 +71,8 @@ def test_ghrl_anneals_match_reference_curves(name):
     thermal loop on a 16^3 GHRL slab (homeotropic, W = 4), a chiral droplet
     (planar anchoring, field along z) and bulk Pear, made by
     tests/golden/make_ghrl_anneals.py.  The
-    GPU runs 32 replicas with the same protocol; the tolerance is that of the
-    oracle's test on these curves (4 combined standard errors + 2e-3 in S,
-    4e-3 in E)."""
+    GPU runs 32 replicas with the same protocol; at every T the means agree
+    within 3 combined standard errors (helpers.stat_parity_failures)."""
     g = json.load(open(os.path.join(os.path.dirname(GOLD), name + ".json")))
     temps, MC, R = g["temps"], g["mct"], 32
     descs = _ghrl_descs(g["model"], temps[0], R)
@@ -92,12 +90,9 @@ def test_ghrl_anneals_match_reference_curves(name):
                 st = eng.stats(r)
                 S[r, t] = st[mcx.ST_S1] / st[mcx.ST_N]
                 E[r, t] = st[mcx.ST_E1] / st[mcx.ST_N]
-    for key, G, tol in (("S", S, 2e-3), ("E", E, 4e-3)):
-        m, se = G.mean(0), G.std(0, ddof=1) / np.sqrt(R)
-        rm, rse = np.array(g[key + "_mean"]), np.array(g[key + "_sem"])
-        sig = np.hypot(se, rse)
-        bad = np.nonzero(np.abs(m - rm) > 4 * sig + tol)[0]
-        assert len(bad) == 0, [(temps[i], m[i], rm[i], sig[i]) for i in bad]
+    for key, G in (("S", S), ("E", E)):
+        bad = stat_parity_failures(G, g, key)
+        assert not bad, [(temps[i], *rest) for i, *rest in bad]
 
 
 def test_droplet_field_sweep_matches_reference_curve():
@@ -105,7 +100,8 @@ def test_droplet_field_sweep_matches_reference_curve():
     electric-field loop (electricEvolveN::run, src/evolve_electric.cpp:28-90)
     on the chiral GHRL droplet at T = 0.8, field stepped 0 -> 2.0 by 0.2; the
     GPU runs 32 replicas with the same protocol (per field value 100 sweeps,
-    then 100 measured ones; step size carried)."""
+    then 100 measured ones; step size carried); 3 combined standard errors at
+    every field value."""
     g = json.load(open(os.path.join(os.path.dirname(GOLD), "ghrl_sphere16_field_sweep.json")))
     fields, MC, R = g["fields"], g["mct"], 32
     descs = _ghrl_descs(g["model"], g["T"], R)
@@ -123,9 +119,6 @@ def test_droplet_field_sweep_matches_reference_curve():
                 st = eng.stats(r)
                 S[r, t] = st[mcx.ST_S1] / st[mcx.ST_N]
                 E[r, t] = st[mcx.ST_E1] / st[mcx.ST_N]
-    for key, G, tol in (("S", S, 2e-3), ("E", E, 4e-3)):
-        m, se = G.mean(0), G.std(0, ddof=1) / np.sqrt(R)
-        rm, rse = np.array(g[key + "_mean"]), np.array(g[key + "_sem"])
-        sig = np.hypot(se, rse)
-        bad = np.nonzero(np.abs(m - rm) > 4 * sig + tol)[0]
-        assert len(bad) == 0, [(fields[i], m[i], rm[i], sig[i]) for i in bad]
+    for key, G in (("S", S), ("E", E)):
+        bad = stat_parity_failures(G, g, key)
+        assert not bad, [(fields[i], *rest) for i, *rest in bad]

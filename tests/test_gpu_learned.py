@@ -94,10 +94,10 @@ def test_learned_pass_parity(name):
 def test_learned_chain_samples_the_same_equilibrium(T):
     """Random (untrained) weights: a poor proposal, but the exact MH ratio
     keeps the Boltzmann distribution -- E and S agree with the plain chain
-    within 4 combined standard errors over 16 replicas each."""
+    within 3 combined standard errors over 32 replicas each."""
     m = O.Model(nx=8, ny=8, nz=8, potential="ll")
     params = _weights(2, scale=1.0)
-    R = 16
+    R = 32
     res = {}
     for kind in ("plain", "vmf_mlp"):
         descs = [desc_from_model(m, T=T, seed=100 + r, stream=r) for r in range(R)]
@@ -116,7 +116,7 @@ def test_learned_chain_samples_the_same_equilibrium(T):
     for q in range(2):
         a, b = res["plain"][q], res["vmf_mlp"][q]
         se = np.sqrt(a.var(ddof=1) / len(a) + b.var(ddof=1) / len(b))
-        assert abs(a.mean() - b.mean()) < 4 * se + 1e-4, (q, a.mean(), b.mean(), se)
+        assert abs(a.mean() - b.mean()) <= 3 * se, (q, a.mean(), b.mean(), se)
 
 
 IDENTITY_CASES = {**CASES,

@@ -193,14 +193,14 @@ def test_training_errors():
 
 def test_trained_proposal_shortens_autocorrelation():
     """What the trained network gains over the method without it, per sweep:
-    LL 16^3 x 16 replicas at T = 1.15, both chains from the same equilibrated
+    LL 16^3 x 32 replicas at T = 1.15, both chains from the same equilibrated
     states with the step size frozen; the learned chain's integrated
     autocorrelation time of S is well below the plain chain's, and the two
-    agree on E and S (exact MH ratio)."""
+    agree on E and S within 3 combined standard errors (exact MH ratio)."""
     from mcx.autocorr import tau_int
     from mcx import gain
     m = O.Model(nx=16, ny=16, nz=16, potential="ll")
-    R, T, n = 16, 1.15, 3000
+    R, T, n = 32, 1.15, 3000
     with mcx.Engine([desc_from_model(m, T=T, seed=70 + r, stream=r) for r in range(R)]) as eng:
         for r in range(R):
             eng.init_random(r, 9 + r)
@@ -224,4 +224,19 @@ def test_trained_proposal_shortens_autocorrelation():
     for q in (1, 2):
         a, b = out["plain"][q], out["vmf_mlp"][q]
         se = np.hypot(a.std(ddof=1), b.std(ddof=1)) / np.sqrt(R)
-        assert abs(a.mean() - b.mean()) < 4 * se + 1e-4
+        assert abs(a.mean() - b.mean()) <= 3 * se, (q, a.mean(), b.mean(), se)
+
+
+def test_learned_and_plain_agree_at_every_c4_temperature():
+    """The learned-proposal protocol of the 96^3 workload (mcx.gain: plain
+    equilibration, training on the plain sampler's states, frozen step, both
+    proposals from the same saved states) on 16^3 lattices: at each of
+    T = 1.00, 1.10, 1.12, 1.15, over 32 replicas, E and S of the two chains
+    agree within 3 combined standard errors, and the trained network shortens
+    the integrated autocorrelation time per sweep."""
+    from mcx import gain
+    res = gain.run(L=16, per_T=32, equil=1500, meas=2000, train_samples=1 << 18,
+                   schedule=((600, 2e-3), (300, 5e-4)), batch=4096, seed=3)
+    for row in res["rows"]:
+        assert row["E_diff_sigma"] <= 3 and row["S_diff_sigma"] <= 3, row
+        assert row["tau_ratio"] > 1.0, row
