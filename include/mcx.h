@@ -382,9 +382,10 @@ mcx_status mcx_check_file(const char *param_file, mcx_replica_desc *desc);
  * with cudaGetSymbolAddress; make that first call before any stream capture.
  * Every call shares the array: calls whose kernels overlap on the GPU (for
  * example on two streams at once) race and give wrong results; calls ordered
- * on one stream are safe.  Lattices above MCX_NOALLOC_MAX_SITES sites are
- * rejected with MCX_ERR_INVALID.  Asynchronous on `stream` (a cudaStream_t,
- * NULL = the default stream). */
+ * on one stream are safe.  Lattices above MCX_NOALLOC_MAX_SITES sites, and
+ * descriptors with an unknown potential (LL, GHRL and Pear are measured) or
+ * anchoring, are rejected with MCX_ERR_INVALID.  Asynchronous on `stream` (a
+ * cudaStream_t, NULL = the default stream). */
 #define MCX_NOALLOC_MAX_BLOCKS 1024
 #define MCX_NOALLOC_MAX_SITES (1 << 27)
 mcx_status mcx_measure_noalloc(const mcx_replica_desc *desc, const float *d_ni_aos, const int *d_pt,
@@ -407,8 +408,11 @@ mcx_status mcx_local_order(mcx_engine *eng, int replica, float *S);
  * (the Philox counters: a loaded engine continues the saved trajectory bit
  * for bit), running sums, and the network weights and proposal when set.  The
  * measured-sweep series and the training optimiser state are not saved.
- * mcx_load needs an engine of the same replica count, sizes, geometries,
- * potentials and bounds. */
+ * mcx_load needs an engine whose replicas have the saved descriptors
+ * (everything but temperature and step size, which are restored: sizes,
+ * geometry, bounds, potential, couplings, field, anchoring, RNG seed and
+ * stream); otherwise MCX_ERR_INVALID.  It reads and checks the whole file
+ * before changing anything, so a failed load leaves the engine as it was. */
 mcx_status mcx_save(mcx_engine *eng, const char *path);
 mcx_status mcx_load(mcx_engine *eng, const char *path);
 

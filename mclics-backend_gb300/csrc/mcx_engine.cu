@@ -1438,6 +1438,9 @@ extern "C" mcx_status mcx_save(mcx_engine *e, const char *path) {
   return MCX_OK;
 }
 
+// Reads and checks the whole checkpoint into host buffers before it touches
+// the engine, so a file that is truncated, made for other replicas or holding
+// an invalid mask or network leaves the engine as it was.
 extern "C" mcx_status mcx_load(mcx_engine *e, const char *path) {
   if (!e || !path) return fail(e, MCX_ERR_INVALID, "mcx_load: null argument");
   FileCloser fc{fopen(path, "rb")};
@@ -1450,53 +1453,86 @@ extern "C" mcx_status mcx_load(mcx_engine *e, const char *path) {
     return fail(e, MCX_ERR_PARSE, "mcx_load: checkpoint version %u / descriptor size %u not supported", hdr[0], hdr[2]);
   if ((int)hdr[1] != e->nrep)
     return fail(e, MCX_ERR_INVALID, "mcx_load: checkpoint holds %u replicas, the engine %d", hdr[1], e->nrep);
-  if (mcx_status st = flush(e)) return st;
-  CK(e, cudaStreamSynchronize(e->stream));
-  std::vector<RepState> st(e->nrep);
-  std::vector<double> stats((size_t)kStats * e->nrep);
-  CK(e, cudaMemcpy(st.data(), e->d_st, sizeof(RepState) * e->nrep, cudaMemcpyDeviceToHost));
-  for (int r = 0; r < e->nrep; r++) {
+  const int n = e->nrep;
+  std::vector<CkptState> cs(n);
+  std::vector<double> stats((size_t)kStats * n);
+  std::vector<std::vector<float>> ni(n), ns(n);
+  std::vector<std::vector<int>> pt(n);
+  for (int r = 0; r < n; r++) {
     const RepDev &R = e->rep[r];
     mcx_replica_desc d;
-    CkptState cs;
-    if (fread(&d, sizeof d, 1, fc.f) != 1 || fread(&cs, sizeof cs, 1, fc.f) != 1 ||
+    if (fread(&d, sizeof d, 1, fc.f) != 1 || fread(&cs[r], sizeof cs[r], 1, fc.f) != 1 ||
         fread(stats.data() + (size_t)kStats * r, sizeof(double), kStats, fc.f) != (size_t)kStats)
       return fail(e, MCX_ERR_PARSE, "mcx_load: %s is truncated", path);
-    const mcx_replica_desc &m = e->desc[r];
-    if (d.nx != m.nx || d.ny != m.ny || d.nz != m.nz || d.geometry != m.geometry || d.potential != m.potential ||
-        d.xbound != m.xbound || d.ybound != m.ybound || d.zbound != m.zbound)
-      return fail(e, MCX_ERR_INVALID, "mcx_load: replica %d of the checkpoint is %dx%dx%d (geometry %d, potential %d), "
-                  "the engine's %dx%dx%d (geometry %d, potential %d)", r, d.nx, d.ny, d.nz, d.geometry, d.potential,
-                  m.nx, m.ny, m.nz, m.geometry, m.potential);
-    std::vector<float> ni(3 * (size_t)R.ntot);
-    if (fread(ni.data(), sizeof(float), ni.size(), fc.f) != ni.size())
+    // the whole descriptor must be the engine's (temperature and step size
+    // are state and come from the checkpoint): another seed or stream would
+    // not continue the saved trajectory, other physics not the saved model
+    mcx_replica_desc a = d, b = e->desc[r];
+    a.T = b.T = 0.f;
+    a.ang_var = b.ang_var = 0.f;
+    if (memcmp(&a, &b, sizeof a) != 0) {
+      const char *what = d.nx != b.nx || d.ny != b.ny || d.nz != b.nz ? "lattice size"
+                         : d.geometry != b.geometry || d.xbound != b.xbound || d.ybound != b.ybound ||
+                                   d.zbound != b.zbound
+                             ? "geometry or bounds"
+                         : d.potential != b.potential ? "pair potential"
+                         : d.seed != b.seed || d.stream != b.stream ? "RNG seed or stream"
+                                                                    : "physical parameters (couplings, field, anchoring)";
+      return fail(e, MCX_ERR_INVALID, "mcx_load: replica %d of the checkpoint differs from the engine's in its %s",
+                  r, what);
+    }
+    ni[r].resize(3 * (size_t)R.ntot);
+    if (fread(ni[r].data(), sizeof(float), ni[r].size(), fc.f) != ni[r].size())
       return fail(e, MCX_ERR_PARSE, "mcx_load: %s is truncated", path);
     if (e->var.mask) {
-      std::vector<int> pt(R.ntot);
-      std::vector<float> ns(3 * (size_t)R.ntot);
-      if (fread(pt.data(), sizeof(int), pt.size(), fc.f) != pt.size() ||
-          fread(ns.data(), sizeof(float), ns.size(), fc.f) != ns.size())
+      pt[r].resize(R.ntot);
+      ns[r].resize(3 * (size_t)R.ntot);
+      if (fread(pt[r].data(), sizeof(int), pt[r].size(), fc.f) != pt[r].size() ||
+          fread(ns[r].data(), sizeof(float), ns[r].size(), fc.f) != ns[r].size())
         return fail(e, MCX_ERR_PARSE, "mcx_load: %s is truncated", path);
-      if (mcx_status s2 = mcx_set_mask(e, r, pt.data(), ns.data())) return s2;
+      long active = 0;
+      for (long q = 0; q < R.ntot; q++) {
+        const int v = pt[r][q];
+        if (v < 0 || v > 255 || (v > 1 && v - 2 >= R.nsurf))
+          return fail(e, MCX_ERR_PARSE, "mcx_load: replica %d: point type %d at site %ld is invalid", r, v, q);
+        active += v != 0;
+      }
+      if (active == 0) return fail(e, MCX_ERR_PARSE, "mcx_load: replica %d: mask has no active site", r);
     }
-    if (mcx_status s2 = mcx_set_state(e, r, ni.data())) return s2;
-    st[r].T = cs.T;
-    st[r].ang_var = cs.ang_var;
-    st[r].sweep = cs.sweep;
-    st[r].meas = cs.meas;
-    st[r].frozen = cs.frozen;
-    st[r].cnt = 0;
-    e->desc[r].T = cs.T;
   }
+  int32_t prop = 0;
+  std::vector<float> w;
   if (hdr[3] & 1u) {
-    int32_t prop = 0;
-    std::vector<float> w(MCX_MLP_PARAMS);
+    w.resize(MCX_MLP_PARAMS);
     if (fread(&prop, sizeof prop, 1, fc.f) != 1 || fread(w.data(), sizeof(float), w.size(), fc.f) != w.size())
       return fail(e, MCX_ERR_PARSE, "mcx_load: %s is truncated", path);
+    if (prop != MCX_PROPOSAL_PLAIN && prop != MCX_PROPOSAL_VMF_MLP)
+      return fail(e, MCX_ERR_PARSE, "mcx_load: unknown proposal %d", prop);
+    if (e->var.pot == POT_PEAR)
+      return fail(e, MCX_ERR_UNSUPPORTED, "mcx_load: the checkpoint holds a network; Pear runs the plain proposal only");
+  }
+  // everything read and checked: apply
+  if (mcx_status st = flush(e)) return st;
+  CK(e, cudaStreamSynchronize(e->stream));
+  std::vector<RepState> st(n);
+  CK(e, cudaMemcpy(st.data(), e->d_st, sizeof(RepState) * n, cudaMemcpyDeviceToHost));
+  for (int r = 0; r < n; r++) {
+    if (e->var.mask)
+      if (mcx_status s2 = mcx_set_mask(e, r, pt[r].data(), ns[r].data())) return s2;
+    if (mcx_status s2 = mcx_set_state(e, r, ni[r].data())) return s2;
+    st[r].T = cs[r].T;
+    st[r].ang_var = cs[r].ang_var;
+    st[r].sweep = cs[r].sweep;
+    st[r].meas = cs[r].meas;
+    st[r].frozen = cs[r].frozen;
+    st[r].cnt = 0;
+    e->desc[r].T = cs[r].T;
+  }
+  if (!w.empty()) {
     if (mcx_status s2 = mcx_set_mlp(e, w.data(), MCX_MLP_PARAMS)) return s2;
     if (mcx_status s2 = mcx_set_proposal(e, prop)) return s2;
   }
-  CK(e, cudaMemcpyAsync(e->d_st, st.data(), sizeof(RepState) * e->nrep, cudaMemcpyHostToDevice, e->stream));
+  CK(e, cudaMemcpyAsync(e->d_st, st.data(), sizeof(RepState) * n, cudaMemcpyHostToDevice, e->stream));
   CK(e, cudaMemcpyAsync(e->d_stats, stats.data(), sizeof(double) * stats.size(), cudaMemcpyHostToDevice, e->stream));
   CK(e, cudaStreamSynchronize(e->stream));
   e->meas_flushed = st[0].meas;

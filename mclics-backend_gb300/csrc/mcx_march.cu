@@ -290,10 +290,12 @@ __global__ void __launch_bounds__(NT, march_min_blocks<POT, false, NT>()) k_tmar
     const bool ok = mbar_wait(&bars[t & 1], (uint32_t)((t >> 1) & 1));
     if (__syncthreads_or(!ok)) {
       // a step's copies never completed: report, let the copies in flight
-      // land (bounded), leave without touching the sums
+      // land (bounded: this step's, and the next step's when they were
+      // issued), leave without touching the sums
       if (threadIdx.x == 0) {
         atomicExch(a.err, 1u);
-        mbar_wait(&bars[(t + 1) & 1], (uint32_t)(((t + 1) >> 1) & 1));
+        mbar_wait(&bars[t & 1], (uint32_t)((t >> 1) & 1));
+        if (t + 1 < L) mbar_wait(&bars[(t + 1) & 1], (uint32_t)(((t + 1) >> 1) & 1));
       }
       return;
     }

@@ -45,6 +45,7 @@ struct NaParams {
   int xb, yb, zb;
   int pot;
   float A, lam, mu, nu, rho, sigma;
+  float B1, C;  // Pear
   float elecA, elecE, ex, ey, ez;
   int nsurf;
   int anch[kMaxSurf];
@@ -56,6 +57,8 @@ struct NaParams {
 __device__ __forceinline__ RepDev as_rep(const NaParams &p) {
   RepDev R;
   R.A = p.A;
+  R.B1 = p.B1;
+  R.C = p.C;
   R.lam = p.lam;
   R.mu = p.mu;
   R.nu = p.nu;
@@ -77,11 +80,20 @@ __device__ __forceinline__ RepDev as_rep(const NaParams &p) {
   return R;
 }
 
+// Bond energy of director a with its neighbour b in slot d (x+, x-, y+, y-,
+// z+, z-; r = +-e_axis): Lebwohl-Lasher, Pear and GHRL (src/potential.cpp:10-38).
 __device__ __forceinline__ float pair_energy(const RepDev &R, int pot, int d, float ax, float ay, float az, float bx,
                                              float by, float bz) {
   if (pot == POT_LL) {
     const float nij = ax * bx + ay * by + az * bz;
     return -1.5f * R.A * nij * nij;
+  }
+  if (pot == POT_PEAR) {
+    // -A nij^2 - B1 nij - (C/4)(1 + 2 nij + nij^2)((b - a) . r)
+    const float nij = ax * bx + ay * by + az * bz;
+    const int x = d >> 1;
+    const float dr = (x == 0 ? bx - ax : (x == 1 ? by - ay : bz - az)) * ((d & 1) ? -1.f : 1.f);
+    return -R.A * nij * nij - R.B1 * nij - (R.C * 0.25f) * ((1.f + 2.f * nij + nij * nij) * dr);
   }
   const float sg = (d & 1) ? -1.f : 1.f;
   switch (d >> 1) {
@@ -254,10 +266,26 @@ extern "C" mcx_status mcx_measure_noalloc(const mcx_replica_desc *desc, const fl
     set_last_error(buf);
     return MCX_ERR_INVALID;
   }
-  if (desc->potential < 0 || desc->potential > 1 || desc->n_surfaces < 0 || desc->n_surfaces > MCX_MAX_SURFACES) {
-    set_last_error("mcx_measure_noalloc: bad potential or surface count");
+  if (desc->potential < MCX_POT_LL || desc->potential > MCX_POT_PEAR) {
+    char buf[120];
+    snprintf(buf, sizeof buf, "mcx_measure_noalloc: unknown potential %d (0 LL, 1 GHRL, 2 Pear)", desc->potential);
+    set_last_error(buf);
     return MCX_ERR_INVALID;
   }
+  if (desc->n_surfaces < 0 || desc->n_surfaces > MCX_MAX_SURFACES) {
+    char buf[120];
+    snprintf(buf, sizeof buf, "mcx_measure_noalloc: surface count %d outside [0, %d]", desc->n_surfaces,
+             MCX_MAX_SURFACES);
+    set_last_error(buf);
+    return MCX_ERR_INVALID;
+  }
+  for (int s = 0; s < desc->n_surfaces; s++)
+    if (desc->anchoring[s] < MCX_ANCH_HOMEOTROPIC || desc->anchoring[s] > MCX_ANCH_STRONG_GHRL) {
+      char buf[120];
+      snprintf(buf, sizeof buf, "mcx_measure_noalloc: unknown anchoring %d on surface %d", desc->anchoring[s], s);
+      set_last_error(buf);
+      return MCX_ERR_INVALID;
+    }
   int dev = 0;
   cudaError_t rc = cudaGetDevice(&dev);
   if (rc != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
@@ -294,6 +322,8 @@ extern "C" mcx_status mcx_measure_noalloc(const mcx_replica_desc *desc, const fl
   if (desc->geometry == MCX_GEO_SPHERE) p.xb = p.yb = p.zb = MCX_BOUND_FREE;
   p.pot = desc->potential;
   p.A = desc->A;
+  p.B1 = desc->B1;
+  p.C = desc->C;
   float g[5] = {0, 0, 1, 0, 0};
   if (desc->potential == MCX_POT_GHRL) ghrl_constants(desc->k11, desc->k22, desc->k33, desc->p0, g);
   p.lam = g[0];

@@ -106,6 +106,46 @@ def test_checkpoint_continues_the_trajectory(tmp_path):
             c.load(path)
 
 
+def test_failed_checkpoint_load_leaves_the_engine_unchanged(tmp_path):
+    """A truncated checkpoint, one made with another seed and one made for
+    other physics are refused, and the engine keeps its own directors, mask,
+    counters and running sums (the file is read and checked before anything
+    is applied)."""
+    m = O.Model(nx=10, ny=8, nz=6, geometry="slab", potential="ghrl", k11=1.0, k22=0.8, k33=1.2,
+                surfaces=[O.Surface("homeotropic", 2.0), O.Surface("fg", 1.0)])
+    descs = [desc_from_model(m, T=0.9, seed=4 + r, stream=r) for r in range(3)]
+    path = str(tmp_path / "ck.bin")
+    with mcx.Engine(descs) as a:
+        for r in range(3):
+            a.init_random(r, 50 + r)
+        a.sweep(5, measure=True)
+        a.save(path)
+    data = open(path, "rb").read()
+    bad = {"truncated": data[:len(data) - 1000]}
+    other_seed = [desc_from_model(m, T=0.9, seed=4 + r + (r == 2), stream=r) for r in range(3)]
+    m2 = O.Model(**{**m.__dict__, "k22": 0.7})
+    other_phys = [desc_from_model(m2, T=0.9, seed=4 + r, stream=r) for r in range(3)]
+    for name, text in bad.items():
+        p = tmp_path / (name + ".bin")
+        p.write_bytes(text)
+        bad[name] = str(p)
+    for engine_descs, ck in ((descs, bad["truncated"]), (other_seed, path), (other_phys, path)):
+        with mcx.Engine(engine_descs) as b:
+            for r in range(3):
+                b.init_random(r, 90 + r)
+            b.sweep(3, measure=True)
+            before = [(b.get_state(r), b.get_mask(r), b.stats(r)) for r in range(3)]
+            with pytest.raises(mcx.McxError):
+                b.load(ck)
+            for r in range(3):
+                ni, (pt, ns), st = before[r]
+                assert np.array_equal(b.get_state(r), ni)
+                gp, gn = b.get_mask(r)
+                assert np.array_equal(gp, pt) and np.array_equal(gn, ns)
+                assert np.array_equal(b.stats(r), st)
+            b.sweep(1)  # still usable
+
+
 def test_replica_exchange_decisions():
     m = O.Model(nx=8, ny=8, nz=8, potential="ll")
     Ts = [0.6, 0.9, 1.2, 1.5]
