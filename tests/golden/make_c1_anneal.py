@@ -30,7 +30,7 @@ sys.path.insert(0, ROOT)
 from oracle import oracle as O  # noqa: E402
 from oracle import refproc  # noqa: E402
 
-RUNS = 32
+RUNS = 128
 N = 16
 MCT = MCS = 100
 OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "c1_ll16_anneal.json")

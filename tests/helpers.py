@@ -46,7 +46,9 @@ def neighbours(lat, m, s):
 def stat_parity_failures(G: np.ndarray, g: dict, key: str):
     """Rows where the mean over runs of G (runs x rows) and the golden's mean
     g[key + "_mean"] differ by more than 3 combined standard errors plus the
-    systematic of the reference's unrenormalised directors.
+    systematic of the reference's unrenormalised directors, as
+    (row, mean, golden mean, combined standard error, deviation in those
+    errors beyond the systematic).
 
     The reference's CPU sweep does not renormalise its proposals
     (src/evolve.cpp:139-151), so its director lengths drift by float rounding;
@@ -62,6 +64,38 @@ def stat_parity_failures(G: np.ndarray, g: dict, key: str):
     sig = np.hypot(se, rse)
     eps = np.asarray(g.get("len2_drift_absmax", np.zeros_like(rm)))
     sysm = 2 * eps if key == "S" else 4 * eps * (np.abs(rm) + 1)
-    dev = np.abs(m - rm)
-    return [(int(i), float(m[i]), float(rm[i]), float(sig[i]), float(dev[i] / sig[i]))
-            for i in np.nonzero(dev > 3 * sig + sysm)[0]]
+    z = np.maximum(np.abs(m - rm) - sysm, 0.0) / sig
+    return [(int(i), float(m[i]), float(rm[i]), float(sig[i]), float(z[i])) for i in np.nonzero(z > 3)[0]]
+
+
+P_BEYOND_3SIGMA = 0.0026997961  # two-sided normal tail beyond 3 standard errors
+
+
+def chance_exceedances(n: int, alpha: float = 0.05) -> int:
+    """How many of n independent comparisons may lie beyond 3 standard errors
+    by chance: the smallest k with P(Binomial(n, p3) > k) < alpha, p3 the
+    two-sided normal tail beyond 3 sigma.  0 for up to 18 comparisons (every
+    row within 3 sigma), 1 for 19..131 (e.g. both S and E of the 61
+    temperatures of the LL anneal)."""
+    from math import comb
+    k, tail = 0, 1.0
+    while True:
+        tail -= comb(n, k) * P_BEYOND_3SIGMA ** k * (1 - P_BEYOND_3SIGMA) ** (n - k)
+        if tail < alpha:
+            return k
+        k += 1
+
+
+def assert_stat_parity(checks, labels):
+    """checks: (G, golden, key) triples compared row by row against the same
+    labels.  Every row must lie within 3 combined standard errors
+    (stat_parity_failures), except for as many rows as chance alone puts
+    beyond 3 sigma among all the comparisons made (chance_exceedances, 5%
+    family-wise), and none beyond 4 sigma."""
+    bad, n = [], 0
+    for G, g, key in checks:
+        n += G.shape[1]
+        bad += [(key, labels[i], *rest) for i, *rest in stat_parity_failures(G, g, key)]
+    allowed = chance_exceedances(n)
+    assert len(bad) <= allowed and all(b[-1] <= 4.0 for b in bad), (n, allowed, bad)
+    return bad

@@ -3,7 +3,7 @@ on reduced GHRL configurations.
 
 tests/golden/c1_ll16_anneal.json holds S(T) and E(T) of the reference's
 thermalEvolveN::run (src/evolve_thermal.cpp:30-99) on LL bulk 16^3, random
-start, Ti = 1.2 -> Tf = 0.0 in steps of -0.02, MCT = MCS = 100, over 32
+start, Ti = 1.2 -> Tf = 0.0 in steps of -0.02, MCT = MCS = 100, over 128
 independent runs (generated by tests/golden/make_c1_anneal.py from the
 reference compiled here).  The GPU runs the same protocol on 32 replicas in
 one engine: per temperature 100 sweeps, then 100 sweeps each followed by the
@@ -12,9 +12,10 @@ E / S measurement, step size carried across temperatures.
 The chains differ (2-colour vs 8-colour order, Philox vs ranlxs0, renormalised
 vs unrenormalised proposals), so the comparison is statistical: at every T the
 means agree within 3 combined standard errors (plus the systematic of the
-reference's director-length drift, measured in its runs and below 1e-5:
-helpers.stat_parity_failures), and chi^2 per temperature over the whole curve
-stays below 2."""
+reference's director-length drift, measured in its runs and below 1e-5),
+except for as many of the 122 comparisons as chance puts beyond 3 sigma at 5%
+family-wise (one) and none beyond 4 sigma (helpers.assert_stat_parity), and
+chi^2 per temperature over the whole curve stays below 2."""
 import json
 import os
 
@@ -22,7 +23,7 @@ import numpy as np
 import pytest
 
 import mcx
-from helpers import stat_parity_failures
+from helpers import assert_stat_parity
 
 pytestmark = pytest.mark.gpu
 
@@ -49,10 +50,9 @@ def test_c1_anneal_matches_reference_curves():
                 st = eng.stats(r)
                 S[r, t] = st[mcx.ST_S1] / st[mcx.ST_N]
                 E[r, t] = st[mcx.ST_E1] / st[mcx.ST_N]
+    assert_stat_parity([(S, g, "S"), (E, g, "E")], temps)
     chi2 = []
     for name, G in (("S", S), ("E", E)):
-        bad = stat_parity_failures(G, g, name)
-        assert not bad, [(temps[i], *rest) for i, *rest in bad]
         m, se = G.mean(0), G.std(0, ddof=1) / np.sqrt(R)
         sig = np.hypot(se, np.array(g[name + "_sem"]))
         chi2.append(float(np.mean(((m - np.array(g[name + "_mean"])) / sig) ** 2)))
@@ -72,7 +72,9 @@ def test_ghrl_anneals_match_reference_curves(name):
     (planar anchoring, field along z) and bulk Pear, made by
     tests/golden/make_ghrl_anneals.py.  The
     GPU runs 32 replicas with the same protocol; at every T the means agree
-    within 3 combined standard errors (helpers.stat_parity_failures)."""
+    within 3 combined standard errors (helpers.assert_stat_parity: one
+    chance exceedance of at most 4 sigma allowed among the 22-26
+    comparisons)."""
     g = json.load(open(os.path.join(os.path.dirname(GOLD), name + ".json")))
     temps, MC, R = g["temps"], g["mct"], 32
     descs = _ghrl_descs(g["model"], temps[0], R)
@@ -90,9 +92,7 @@ def test_ghrl_anneals_match_reference_curves(name):
                 st = eng.stats(r)
                 S[r, t] = st[mcx.ST_S1] / st[mcx.ST_N]
                 E[r, t] = st[mcx.ST_E1] / st[mcx.ST_N]
-    for key, G in (("S", S), ("E", E)):
-        bad = stat_parity_failures(G, g, key)
-        assert not bad, [(temps[i], *rest) for i, *rest in bad]
+    assert_stat_parity([(S, g, "S"), (E, g, "E")], temps)
 
 
 def test_droplet_field_sweep_matches_reference_curve():
@@ -101,7 +101,7 @@ def test_droplet_field_sweep_matches_reference_curve():
     on the chiral GHRL droplet at T = 0.8, field stepped 0 -> 2.0 by 0.2; the
     GPU runs 32 replicas with the same protocol (per field value 100 sweeps,
     then 100 measured ones; step size carried); 3 combined standard errors at
-    every field value."""
+    every field value (helpers.assert_stat_parity)."""
     g = json.load(open(os.path.join(os.path.dirname(GOLD), "ghrl_sphere16_field_sweep.json")))
     fields, MC, R = g["fields"], g["mct"], 32
     descs = _ghrl_descs(g["model"], g["T"], R)
@@ -119,6 +119,4 @@ def test_droplet_field_sweep_matches_reference_curve():
                 st = eng.stats(r)
                 S[r, t] = st[mcx.ST_S1] / st[mcx.ST_N]
                 E[r, t] = st[mcx.ST_E1] / st[mcx.ST_N]
-    for key, G in (("S", S), ("E", E)):
-        bad = stat_parity_failures(G, g, key)
-        assert not bad, [(fields[i], *rest) for i, *rest in bad]
+    assert_stat_parity([(S, g, "S"), (E, g, "E")], fields)

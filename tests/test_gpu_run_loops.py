@@ -19,6 +19,7 @@ import numpy as np
 import pytest
 
 import mcx
+from helpers import assert_stat_parity
 
 pytestmark = pytest.mark.gpu
 
@@ -60,11 +61,9 @@ def test_run_file_matches_reference_program(name, tmp_path):
     got = sorted(f for f in os.listdir(out) if f.startswith("director_field_"))
     assert got == g["snapshots"]
     assert (out / "ic.csv").exists()
-    # statistics: S and E per row within 3 combined standard errors
+    # statistics: S and E per row within 3 combined standard errors (at most
+    # 10 comparisons per file: no chance exceedance is allowed)
     vals = np.array(vals)  # [replica, row, (S, varS, E, varE)]
-    mean, sem = vals.mean(0), vals.std(0, ddof=1) / np.sqrt(runs)
     rm, rs = np.array(g["mean"]), np.array(g["sem"])
-    for col in (0, 2):
-        sig = np.sqrt(sem[:, col] ** 2 + rs[:, col] ** 2)
-        dev = np.abs(mean[:, col] - rm[:, col])
-        assert np.all(dev <= 3 * sig), (g["columns"][col], g["labels"], mean[:, col], rm[:, col], sig)
+    gold = {"S_mean": rm[:, 0], "S_sem": rs[:, 0], "E_mean": rm[:, 2], "E_sem": rs[:, 2]}
+    assert_stat_parity([(vals[:, :, 0], gold, "S"), (vals[:, :, 2], gold, "E")], g["labels"])
