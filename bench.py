@@ -24,7 +24,15 @@ One step = one temperature block (4000 red/black sweeps of 2,097,152 sites,
              (mcx_pass_timing) right after the timed region.
   cpu_baseline  the reference CPU path on the host cores on a bounded sample
              of the same lattice (the reference's own EvolveN::Monte_Carlo_Step
-             when oracle/_ref is loadable, else the oracle's C port of it).
+             when oracle/_ref is loadable, else its C port, oracle/mcx_port.c,
+             which reproduces the reference's sweeps bit for bit and runs
+             within 10% of its speed); the host CPU model is recorded.
+  c3, c5, indep_samples  the other configurations, each a bounded run after
+             the headline (--no-workloads skips them): the 256-replica GHRL
+             slab batch and the droplet field sweep (site-updates/s and the
+             masked pass's roofline), and the learned proposal against the
+             plain one on 128 x 96^3 at T = 1.00, 1.10, 1.12, 1.15
+             (effectively independent samples/s by tau_int of E and S).
 
 --impl reference times only that CPU path, per step a bounded sample.
 Multi-GPU runs (torchrun) are replicas: each rank anneals its own lattice.
@@ -61,6 +69,13 @@ FORMS = {"march": ("k_march<LL> (red/black pass)", "z-march"),
          "staged": ("k_tpass<LL> (red/black pass)", "staged pass")}
 WORKLOAD = ("LL bulk 128^3 periodic, A=1, homogeneous ic along z, anneal Ti=1.20 -> Tf=0.90 dT=-0.01, "
             "MCT=2000 MCS=2000 per temperature")
+# dram__bytes_read.sum + dram__bytes_write.sum per launch of the pass kernel
+# on the 128^3 lattice, from one ncu capture (cold-cache replay: every launch
+# starts with the lattice outside L2; in the timed run it stays L2-resident)
+NCU_DRAM_BYTES_128 = {
+    "march": (25.19e6, "ncu capture of k_march<LL> on 128^3 (dram__bytes_read.sum + dram__bytes_write.sum, "
+                       "cold-cache replay)"),
+}
 
 
 def temperatures():
@@ -134,6 +149,24 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def host_cpu() -> str:
+    """The host's CPU model (lscpu's "Model name", else /proc/cpuinfo)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.strip().lower().startswith("model name"):
+                return ln.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        for ln in open("/proc/cpuinfo"):
+            if ln.lower().startswith(("model name", "cpu model")):
+                return ln.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return "unknown"
+
+
 def cpu_baseline(seconds: float = 12.0):
     """Site-updates/s of the reference CPU sweep on the host cores, on a
     bounded sample of the same 128^3 lattice (homogeneous along z, T = 1.20)."""
@@ -183,25 +216,73 @@ def _cpu_reference(seconds, cores):
     n, dt = q.get(timeout=seconds * 20 + 120)
     p.join()
     return {"value": n * SITES / dt, "unit": "site-updates/s", "cores": cores, "kind": "reference",
-            "sample": f"{n} sweeps of the 128^3 LL lattice at T=1.20 (reference EvolveN::Monte_Carlo_Step, "
+            "cpu_model": host_cpu(),
+            "sample": f"{n} sweeps of the {NX}^3 LL lattice at T=1.20 (reference EvolveN::Monte_Carlo_Step, "
                       f"8-colour OpenMP, test-only GSL shim RNG), {dt:.1f} s"}
 
 
-def _cpu_port(seconds, cores):
+def _port(cores):
+    """The reference's sweep ported operation for operation (oracle/mcx_port.c),
+    on a homogeneous 128^3 LL lattice, with one generator per host thread."""
     from oracle import oracle as O
-    m = O.Model(nx=NX, ny=NY, nz=NZ)
     os.environ["OMP_NUM_THREADS"] = str(cores)  # before the oracle library's OpenMP runtime loads
-    lat = O.Lattice(m)
-    a = np.float32(0.5)
-    lat.sweep(TI, a, 1, 0, 0, "eight", O.F_PARALLEL | O.F_NO_NORMALIZE)
+    lat = O.Lattice(O.Model(nx=NX, ny=NY, nz=NZ))
+    return O.Port(lat, seed=1, threads=cores)
+
+
+def _cpu_port(seconds, cores):
+    port = _port(cores)
+    a = port.sweep(TI, 0.5)[1]
     n, t0 = 0, time.perf_counter()
     while time.perf_counter() - t0 < seconds or n < 2:
-        _, a = lat.sweep(TI, a, 1, 0, n + 1, "eight", O.F_PARALLEL | O.F_NO_NORMALIZE)
+        a = port.sweep(TI, a)[1]
         n += 1
     dt = time.perf_counter() - t0
     return {"value": n * SITES / dt, "unit": "site-updates/s", "cores": cores, "kind": "port",
-            "sample": f"{n} sweeps of the 128^3 LL lattice at T=1.20 (oracle C port of "
-                      f"EvolveN::Monte_Carlo_Step, 8-colour, OpenMP), {dt:.1f} s"}
+            "cpu_model": host_cpu(),
+            "sample": f"{n} sweeps of the {NX}^3 LL lattice at T=1.20 (C port of EvolveN::Monte_Carlo_Step: "
+                      f"the reference's float/double arithmetic, 8-colour OpenMP loop and per-thread generators; "
+                      f"bit-identical to the reference's own build on one thread, within 10% of its speed), "
+                      f"{dt:.1f} s"}
+
+
+def other_workloads():
+    """Bounded runs of the configurations beside the headline anneal, each
+    with what it reduces from the full configuration named."""
+    from mcx import gain, workloads
+    out = {}
+    c3 = workloads.run_c3(replicas=256, sweeps=50, steps=3)
+    out["c3"] = {"workload": "256 GHRL slab replicas, sides 16-64, homeotropic W=4, T in [0.8, 1.2], random ic",
+                 "reduced": "3 blocks of 50 + 50 sweeps (the configuration runs 1000 + 1000)",
+                 "site_updates_per_s": c3["site_updates_per_s"], "sweep_ms": c3["sweep_ms"],
+                 "pass_kernel": c3["pass_kernel"], "roofline": c3["roofline"]}
+    c5 = {}
+    for prop in ("vmf_mlp", "plain"):
+        r = workloads.run_c5(replicas=64, sweeps=20, proposal=prop)
+        c5[prop] = {k: r[k] for k in ("site_updates_per_s", "active_site_updates_per_s", "acceptance",
+                                      "pass_kernel", "seconds") if k in r}
+        if "train_loss" in r:
+            c5[prop]["train_loss_first_last"] = r["train_loss"]
+    out["c5"] = {"workload": "64 droplets r=40 in 96^3, GHRL p0=20, planar W=1, field E=0..2.0 by 0.1 at T=0.8",
+                 "reduced": "20 + 20 sweeps per field value (the configuration runs 1000 + 1000)", **c5}
+    g = gain.run(L=96, per_T=32, equil=3000, meas=4000, train_samples=1_000_000)
+    rows = []
+    for r in g["rows"]:
+        p, lrn = r["plain"], r["vmf_mlp"]
+        rows.append({"T": r["T"], "tau_plain": [p["tau_E"], p["tau_S"]], "tau_learned": [lrn["tau_E"], lrn["tau_S"]],
+                     "acceptance": [p["acceptance"], lrn["acceptance"]],
+                     "indep_samples_per_s": [p["indep_samples_per_s"], lrn["indep_samples_per_s"]],
+                     "gain": r["gain"], "E_diff_sigma": r["E_diff_sigma"], "S_diff_sigma": r["S_diff_sigma"],
+                     "tau_reliable": p["reliable"] and lrn["reliable"]})
+    out["indep_samples"] = {
+        "workload": "LL bulk 96^3 periodic, 32 replicas at each of T = 1.00, 1.10, 1.12, 1.15; learned vMF "
+                    "proposal (19-64-64-4 BF16 MLP trained on 10^6 plain-sampler samples) vs plain Metropolis",
+        "reduced": "3000 equilibration and 4000 measured sweeps per proposal (the full protocol: 6000 and 12000)",
+        "metric": "replicas x sweeps/s / (2 max(tau_E, tau_S)), tau_int by Madras-Sokal windowing",
+        "sweeps_per_s": g["sweeps_per_s"], "site_updates_per_s": g["site_updates_per_s"],
+        "mlp_tflops": g["mlp_tflops"], "rows": rows,
+        "gain_min": min(r["gain"] for r in rows), "parity_3sigma": g["parity_3sigma"]}
+    return out
 
 
 def run_reference(args, ws, rank):
@@ -224,16 +305,12 @@ def run_reference(args, ws, rank):
                 times.append(SITES / r["value"] * 2)
         sample = 2
     else:
-        os.environ["OMP_NUM_THREADS"] = str(cores)  # before the oracle library's OpenMP runtime loads
-        from oracle import oracle as O
-        lat = O.Lattice(O.Model(nx=NX, ny=NY, nz=NZ))
-        a = np.float32(0.5)
-        sweep = 0
+        port = _port(cores)
+        a = 0.5
         for s in range(args.warmup + args.steps):
             t0 = time.perf_counter()
             for _ in range(sample):
-                _, a = lat.sweep(TI, a, 1, 0, sweep, "eight", O.F_PARALLEL | O.F_NO_NORMALIZE)
-                sweep += 1
+                a = port.sweep(TI, a)[1]
             if s >= args.warmup:
                 times.append(time.perf_counter() - t0)
     per_step = float(np.mean(times))
@@ -241,10 +318,14 @@ def run_reference(args, ws, rank):
     line = {
         "impl": "reference", "metric": "site-updates/s", "value": value, "unit": "site-updates/s", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_step * 1e3, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32" if use_ref else "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "step": f"bounded sample: {sample} sweeps of the {NX}^3 lattice at T=1.20"},
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "step": f"bounded sample: {sample} sweeps of the {NX}^3 lattice at T=1.20 "
+                                                 f"(the same per-site-update metric as the headline's anneal block)"},
         "cpu_baseline": {"value": value, "unit": "site-updates/s", "cores": cores, "kind": kind,
-                         "sample": f"{sample} sweeps per step, all {cores} host threads"},
+                         "cpu_model": host_cpu(),
+                         "sample": f"{sample} sweeps per step, all {cores} host threads"
+                                   + ("" if use_ref else "; C port of the reference's sweep (bit-identical to its "
+                                                         "own build on one thread, within 10% of its speed)")},
         "e2e": {"value": value, "unit": "site-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -258,6 +339,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-workloads", action="store_true",
+                    help="skip the bounded runs of the other configurations (c3, c5, learned vs plain)")
     ap.add_argument("--side", type=int, default=128,
                     help="lattice side (default 128, the headline workload; other sides are for profiling)")
     ap.add_argument("--sweeps", type=int, default=2000,
@@ -397,12 +480,12 @@ def main():
     from mcx.gain import MLP_FLOP_PER_UPDATE
     flops_per_launch = MLP_FLOP_PER_UPDATE * SITES * R / 2  # one colour: half the sites
     mlp_tflops = flops_per_launch / (per_launch_ms * 1e-3) / 1e12
-    traffic = None
-    tpath = os.path.join(ROOT, "profiles", f"sweep_pass_ll{NX}.md" if R == 1 else f"sweep_pass_ll{NX}x{R}.md")
-    if os.path.exists(tpath):
-        for ln in open(tpath):
-            if ln.startswith("dram_bytes_per_launch:"):
-                traffic = float(ln.split(":", 1)[1].split()[0])
+    # DRAM bytes per launch cannot be counted inside the timed run; for the
+    # headline lattice they come from one ncu capture of this kernel (and are
+    # labelled so), for other shapes they are not reported
+    traffic, traffic_src = None, "not measured for this lattice"
+    if NX == 128 and R == 1 and args.proposal == "plain" and form in NCU_DRAM_BYTES_128:
+        traffic, traffic_src = NCU_DRAM_BYTES_128[form]
 
     # end to end through the C ABI with pinned host buffers
     e2e = None
@@ -441,6 +524,11 @@ def main():
             dist.destroy_process_group()
         return
     cpu = None if args.no_cpu_baseline or ws > 1 else cpu_baseline()
+    headline = NX == 128 and R == 1 and MCT == 2000 and args.proposal == "plain"
+    extra = {}
+    if headline and ws == 1 and not args.no_workloads:
+        eng.close()
+        extra = other_workloads()
     line = {
         "metric": "site-updates/s", "value": value, "unit": "site-updates/s", "n_gpus": ws, "steps": nsteps,
         "warmup": args.warmup, "ms_per_step": per_step_ms, "higher_is_better": True, "scaling": "weak",
@@ -457,7 +545,8 @@ def main():
                                    if args.proposal == "plain" else "learned-proposal z-march (k_lmarch, BF16 MLP)"),
                    "S_E_last_step": [rows[-1][0], rows[-1][1], rows[-1][2]] if rows else None},
         "roofline": ({"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                      "traffic": traffic, "peak_source": peak_src, "kernel": FORMS[form][0],
+                      "traffic": traffic, "traffic_source": traffic_src, "peak_source": peak_src,
+                      "kernel": FORMS[form][0],
                       "bytes_per_launch": bytes_per_launch}
                      if args.proposal == "plain" else
                      # the learned pass is bound by its BF16 MLP: 11.1 kFLOP per site-update against
@@ -477,6 +566,7 @@ def main():
         "e2e": e2e,
         "clocks": clk,
         "gpu_launches": launches,
+        **extra,
     }
     print(json.dumps(line), flush=True)
     eng.close()

@@ -70,6 +70,11 @@ long orc_sweep(const orc_params *p, float *ni, const int *pt, const float *ns, f
 double orc_eigmax(const double Q[9], double vec[3]);
 void orc_measure(const orc_params *p, const float *ni, const int *pt, const float *ns, double out[16]);
 void orc_geometry(int nx, int ny, int nz, int kind, float radius, int *pt, float *ns);
+/* mcx_port.c: the reference's CPU sweep ported operation for operation (its
+ * float / double arithmetic and 8-colour OpenMP loop), for timing. */
+void *orc_port_rngs(unsigned long seed, int threads);
+long orc_port_sweep(const orc_params *p, float *ni, const int *pt, const float *ns, float T, float *ang_var,
+                    long vallid, void *rngs, int threads, float *scratch);
 
 #ifdef __cplusplus
 }

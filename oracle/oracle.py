@@ -197,6 +197,12 @@ def lib():
         L.orc_eigmax.restype = D
         L.orc_measure.argtypes = [P, V, V, V, V]
         L.orc_geometry.argtypes = [I, I, I, I, F, V, V]
+        L.orc_count_valid.argtypes = [P, V]
+        L.orc_count_valid.restype = C.c_long
+        L.orc_port_rngs.argtypes = [C.c_ulong, I]
+        L.orc_port_rngs.restype = V
+        L.orc_port_sweep.argtypes = [P, V, V, V, F, C.POINTER(F), C.c_long, V, I, V]
+        L.orc_port_sweep.restype = C.c_long
         _lib = L
     return _lib
 
@@ -215,6 +221,31 @@ def philox(ctr: Sequence[int], key: Sequence[int]) -> np.ndarray:
     out = np.zeros(4, dtype=np.uint32)
     lib().orc_philox(_ptr(c), _ptr(k), _ptr(out))
     return out
+
+
+class Port:
+    """The reference's CPU sweep ported operation for operation (mcx_port.c:
+    EvolveN::Monte_Carlo_Step with its float / double arithmetic, 8-colour
+    OpenMP loop and per-thread generators), on a Lattice's field: the CPU
+    baseline where the reference's own build is absent."""
+
+    def __init__(self, lat: "Lattice", seed: int = 1, threads: int = 1):
+        import atexit
+        self.lat = lat
+        self.threads = max(1, int(threads))
+        self._rngs = lib().orc_port_rngs(seed, self.threads)
+        self._scratch = np.zeros_like(lat.ni)
+        self.valid = lib().orc_count_valid(C.byref(lat.p), _ptr(lat.pt))
+        libc = C.CDLL(None)
+        libc.free.argtypes = [C.c_void_p]
+        atexit.register(libc.free, self._rngs)
+
+    def sweep(self, T: float, ang_var: float):
+        a = C.c_float(ang_var)
+        L = self.lat
+        acc = lib().orc_port_sweep(C.byref(L.p), _ptr(L.ni), _ptr(L.pt), _ptr(L.ns), T, C.byref(a), self.valid,
+                                   self._rngs, self.threads, _ptr(self._scratch))
+        return acc, a.value
 
 
 class Lattice:
