@@ -65,6 +65,7 @@ FORMS = {"march": ("k_march<LL> (red/black pass)", "z-march"),
          "march_async": ("k_amarch<LL> (red/black pass, cp.async prefetch)", "z-march with cp.async prefetch"),
          "march_tma": ("k_tmarch<LL> (red/black pass, bulk-copy staged)", "z-march with bulk-copy staging"),
          "march_persistent": ("k_pmarch<LL> (red/black passes, one cooperative launch)", "persistent z-march"),
+         "march_quad": ("k_qmarch<LL> (red/black pass, four sites per thread)", "z-march with four sites per thread"),
          "direct": ("k_pass<LL> (red/black pass)", "direct pass"),
          "staged": ("k_tpass<LL> (red/black pass)", "staged pass")}
 WORKLOAD = ("LL bulk 128^3 periodic, A=1, homogeneous ic along z, anneal Ti=1.20 -> Tf=0.90 dT=-0.01, "

@@ -238,7 +238,10 @@ int mcx_get_staged(const mcx_engine *eng);
  *                    batches only);
  *   MCX_PASS_MARCH_PERSISTENT  the z-march as one cooperative launch per run
  *                    of sweeps, its passes separated by grid barriers (blocks
- *                    of 128 or 256 threads; one wave of units).
+ *                    of 128 or 256 threads; one wave of units);
+ *   MCX_PASS_MARCH_QUAD  the z-march with four same-colour sites (two pairs)
+ *                    per thread and 16-byte loads (unmasked batches with nx a
+ *                    multiple of 8).
  * No counterpart in the reference. */
 typedef enum {
   MCX_PASS_MARCH = 0,
@@ -246,7 +249,8 @@ typedef enum {
   MCX_PASS_STAGED = 2,
   MCX_PASS_MARCH_TMA = 3,
   MCX_PASS_MARCH_ASYNC = 4,
-  MCX_PASS_MARCH_PERSISTENT = 5
+  MCX_PASS_MARCH_PERSISTENT = 5,
+  MCX_PASS_MARCH_QUAD = 6
 } mcx_pass_kind;
 mcx_status mcx_set_pass(mcx_engine *eng, int kind);
 int mcx_get_pass(const mcx_engine *eng);

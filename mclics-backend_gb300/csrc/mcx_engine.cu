@@ -75,6 +75,7 @@ struct mcx_engine {
   bool tmarch = false;  // the z-march with rows staged by bulk copies (unmasked lattices)
   bool amarch = false;  // the z-march with a per-thread cp.async prefetch (unmasked LL / GHRL)
   bool pmarch = false;  // the z-march as one cooperative launch per run of sweeps (grid barriers)
+  bool qmarch = false;  // the z-march with four sites per thread (unmasked, nx a multiple of 8)
   // per replica of a masked batch, row j + ny * k: 0 no active site, 1 only
   // bulk sites (point type 1), 2 anything else (empty: unknown)
   std::vector<std::vector<uint8_t>> rowact;
@@ -100,6 +101,7 @@ struct mcx_engine {
 static void drop_graphs(mcx_engine *e);
 static PassArgs pass_args(mcx_engine *e);
 static bool use_tmarch(mcx_engine *e, bool on);
+static bool qmarch_ok(const mcx_engine *e);
 static mcx_status apply_march_shape(mcx_engine *e, int nt, int k);
 
 static mcx_status fail(mcx_engine *e, mcx_status st, const char *fmt, ...) {
@@ -279,12 +281,16 @@ static int unit_class(const mcx_engine *e, const int4 &u, int nt) {
   return seen == 1u ? kUnitDead : (seen == 2u ? kUnitBulk : 0);
 }
 
-static bool unit_dead(const mcx_engine *e, const int4 &u) { return unit_class(e, u, e->march_nt) == kUnitDead; }
+// Site pairs of a plane per z-march work unit: one per thread, two per thread
+// in the four-site form.
+static int unit_pairs(const mcx_engine *e) { return e->qmarch ? 2 * e->march_nt : e->march_nt; }
+
+static bool unit_dead(const mcx_engine *e, const int4 &u) { return unit_class(e, u, unit_pairs(e)) == kUnitDead; }
 
 // Flags of the z-march units and of the learned z-march's units (which only
 // use kUnitDead).
 static void mark_dead_units(mcx_engine *e) {
-  for (int4 &u : e->units) u.w = (u.w & kUnitPlanes) | unit_class(e, u, e->march_nt);
+  for (int4 &u : e->units) u.w = (u.w & kUnitPlanes) | unit_class(e, u, unit_pairs(e));
   for (int4 &u : e->lunits) {
     const int cls = unit_class(e, u, lmarch_block_threads());
     u.w = (u.w & kUnitPlanes) | (cls == kUnitDead ? kUnitDead : 0);
@@ -293,7 +299,7 @@ static void mark_dead_units(mcx_engine *e) {
 
 static void plan_march(mcx_engine *e) {
   e->units.clear();
-  const int nt = e->march_nt;
+  const int nt = e->march_nt, np = unit_pairs(e);
   double avg = 0.0;  // balanced: planes per unit
   const int march_k = e->pmarch ? 0 : e->march_k;
   if (march_k <= 0) {
@@ -302,6 +308,7 @@ static void plan_march(mcx_engine *e) {
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     const int per_sm = e->pmarch   ? pmarch_blocks_per_sm(e->var, nt)
                        : e->amarch ? amarch_blocks_per_sm(e->var, nt)
+                       : e->qmarch ? qmarch_blocks_per_sm(e->var, nt)
                                    : march_blocks_per_sm(e->var, MODE_SWEEP, nt);
     // the persistent form needs every unit resident at once: one wave
     const long long slots = (long long)std::max(1, nsm) * std::max(1, per_sm) * (e->pmarch ? 1 : std::max(1, -e->march_k));
@@ -311,7 +318,7 @@ static void plan_march(mcx_engine *e) {
     for (int r = 0; r < e->nrep; r++) {
       const RepDev &R = e->rep[r];
       const int npp = R.hp * R.ny;
-      for (int p0 = 0; p0 < npp; p0 += nt)
+      for (int p0 = 0; p0 < npp; p0 += np)
         for (int k = 0; k < R.nz; k++)
           work += e->pmarch || !unit_dead(e, make_int4(r, p0, k, 1)) ? 1 : 0;
     }
@@ -324,7 +331,7 @@ static void plan_march(mcx_engine *e) {
     if (march_k > 0) {
       const int K = std::min(march_k, R.nz);
       for (int k0 = 0; k0 < R.nz; k0 += K)
-        for (int p0 = 0; p0 < npp; p0 += nt) {
+        for (int p0 = 0; p0 < npp; p0 += np) {
           e->units.push_back(make_int4(r, p0, k0, std::min(K, R.nz - k0)));
           R.mcta++;
         }
@@ -333,7 +340,7 @@ static void plan_march(mcx_engine *e) {
       const int chunks = std::max(1, std::min(R.nz, (int)std::floor(R.nz / avg)));
       for (int q = 0; q < chunks; q++) {
         const int k0 = (int)((long long)q * R.nz / chunks), k1 = (int)((long long)(q + 1) * R.nz / chunks);
-        for (int p0 = 0; p0 < npp; p0 += nt) {
+        for (int p0 = 0; p0 < npp; p0 += np) {
           e->units.push_back(make_int4(r, p0, k0, k1 - k0));
           R.mcta++;
         }
@@ -785,6 +792,7 @@ static void launch_sweep_pass(mcx_engine *e, PassArgs &pa, int colour, bool meas
   } else if (e->staged) launch_tpass(e->var, mode, pa, e->grid[measure ? 1 : 0], e->stream);
   else if (e->march && e->tmarch) launch_tmarch(e->var, mode, pa, e->march_nt, e->pdl, e->stream);
   else if (e->march && e->amarch) launch_amarch(e->var, mode, pa, e->march_nt, e->pdl, e->stream);
+  else if (e->march && e->qmarch) launch_qmarch(e->var, mode, pa, e->march_nt, e->pdl, e->stream);
   else if (e->march) launch_march(e->var, mode, pa, e->march_nt, e->pdl, e->stream);
   else launch_pass(e->var, mode, pa, e->pgrid[mode], e->stream);
 }
@@ -902,7 +910,7 @@ extern "C" mcx_status mcx_sync(mcx_engine *e) {
 
 extern "C" mcx_status mcx_set_pass(mcx_engine *e, int kind) {
   if (!e) return fail(nullptr, MCX_ERR_INVALID, "null engine");
-  if (kind < MCX_PASS_MARCH || kind > MCX_PASS_MARCH_PERSISTENT)
+  if (kind < MCX_PASS_MARCH || kind > MCX_PASS_MARCH_QUAD)
     return fail(e, MCX_ERR_INVALID, "unknown pass kernel %d", kind);
   if (kind == MCX_PASS_STAGED && !e->can_stage)
     return fail(e, MCX_ERR_UNSUPPORTED, "a replica's rows do not fit the staged pass's shared memory");
@@ -913,12 +921,15 @@ extern "C" mcx_status mcx_set_pass(mcx_engine *e, int kind) {
     return fail(e, MCX_ERR_UNSUPPORTED, "the prefetching z-march needs an unmasked LL or GHRL batch");
   if (kind == MCX_PASS_MARCH_PERSISTENT && !pmarch_block_ok(e->march_nt))
     return fail(e, MCX_ERR_UNSUPPORTED, "the persistent z-march runs blocks of 128 or 256 threads");
+  if (kind == MCX_PASS_MARCH_QUAD && !qmarch_ok(e))
+    return fail(e, MCX_ERR_UNSUPPORTED, "the four-site z-march needs an unmasked batch with nx a multiple of 8");
   if (kind != MCX_PASS_MARCH_TMA) e->tmarch = false;
   e->amarch = kind == MCX_PASS_MARCH_ASYNC;
+  e->qmarch = kind == MCX_PASS_MARCH_QUAD;
   e->pmarch = kind == MCX_PASS_MARCH_PERSISTENT;
   e->staged = kind == MCX_PASS_STAGED;
   e->march = kind == MCX_PASS_MARCH || kind == MCX_PASS_MARCH_TMA || kind == MCX_PASS_MARCH_ASYNC ||
-             kind == MCX_PASS_MARCH_PERSISTENT;
+             kind == MCX_PASS_MARCH_PERSISTENT || kind == MCX_PASS_MARCH_QUAD;
   if (e->march) {
     if (mcx_status st = apply_march_shape(e, e->march_nt, e->march_k)) return st;  // chunks follow the form's residency
     if (e->pmarch && !pmarch_fits(e)) {
@@ -937,6 +948,7 @@ extern "C" int mcx_get_pass(const mcx_engine *e) {
   if (e->staged) return MCX_PASS_STAGED;
   if (!e->march) return MCX_PASS_DIRECT;
   if (e->pmarch) return MCX_PASS_MARCH_PERSISTENT;
+  if (e->qmarch) return MCX_PASS_MARCH_QUAD;
   return e->tmarch ? MCX_PASS_MARCH_TMA : (e->amarch ? MCX_PASS_MARCH_ASYNC : MCX_PASS_MARCH);
 }
 
@@ -991,6 +1003,15 @@ static void plan_tmarch_slots(mcx_engine *e) {
   e->tm_a = (int)align_up(a, 32);
 }
 
+// The four-site z-march runs unmasked batches whose rows hold whole quads
+// of same-colour sites (nx a multiple of 8).
+static bool qmarch_ok(const mcx_engine *e) {
+  if (e->var.mask) return false;
+  for (const RepDev &R : e->rep)
+    if (R.nx % 8) return false;
+  return qmarch_prepare(e->var, e->march_nt);
+}
+
 // Selects the TMA-staged form of the z-march when it can run (unmasked
 // lattices whose slots fit in shared memory).
 static bool use_tmarch(mcx_engine *e, bool on) {
@@ -1008,6 +1029,7 @@ static mcx_status apply_march_shape(mcx_engine *e, int nt, int k) {
   e->march_k = k;
   const size_t before = e->units.size();
   if (e->amarch) e->amarch = amarch_prepare(e->var, nt);  // before planning: its residency sets the waves
+  if (e->qmarch) e->qmarch = qmarch_ok(e);
   plan_march(e);
   if (e->tmarch) use_tmarch(e, true);
   if (e->units.size() > before || !e->d_units) {
@@ -1034,6 +1056,7 @@ extern "C" mcx_status mcx_set_march_shape(mcx_engine *e, int block, int planes) 
 static void launch_march_form(mcx_engine *e, int form, const PassArgs &pa, int nt) {
   if (form == 1) launch_tmarch(e->var, MODE_SWEEP, pa, nt, e->pdl, e->stream);
   else if (form == 2) launch_amarch(e->var, MODE_SWEEP, pa, nt, e->pdl, e->stream);
+  else if (form == 4) launch_qmarch(e->var, MODE_SWEEP, pa, nt, e->pdl, e->stream);
   else launch_march(e->var, MODE_SWEEP, pa, nt, e->pdl, e->stream);
 }
 
@@ -1051,7 +1074,8 @@ extern "C" mcx_status mcx_autotune(mcx_engine *e, int *block, int *planes, float
   const size_t ring_n = (size_t)e->nrep * (e->ring_cap + 1) * kLanes * kQ;
   cudaEvent_t t0, t1;
   mcx_status st = MCX_OK;
-  int best_nt = e->march_nt, best_k = e->march_k, best_form = e->pmarch ? 3 : (e->tmarch ? 1 : (e->amarch ? 2 : 0));
+  int best_nt = e->march_nt, best_k = e->march_k,
+      best_form = e->pmarch ? 3 : (e->tmarch ? 1 : (e->amarch ? 2 : (e->qmarch ? 4 : 0)));
   float best = 1e30f;
 #define CKA(call)                                                                                    \
   do {                                                                                               \
@@ -1073,8 +1097,9 @@ extern "C" mcx_status mcx_autotune(mcx_engine *e, int *block, int *planes, float
     const int nts[3] = {64, 128, 256};
     const int ks[10] = {1, 2, 4, 8, 16, 32, 0, -2, -3, -4};  // fixed depths, then balanced over 1..4 waves
     // forms: 0 the register march, 1 rows staged by bulk copies, 2 the per-thread prefetch,
-    // 3 one cooperative launch per run of sweeps (one wave of units: a single shape per block size)
-    for (int form = 0; form < 4; form++)
+    // 3 one cooperative launch per run of sweeps (one wave of units: a single shape per block size),
+    // 4 four sites per thread
+    for (int form = 0; form < 5; form++)
     for (int a = 0; a < 3; a++)
       for (int ki = 0; ki < 10; ki++) {
         const int k = ks[ki];
@@ -1083,8 +1108,10 @@ extern "C" mcx_status mcx_autotune(mcx_engine *e, int *block, int *planes, float
         e->tmarch = form == 1;
         e->amarch = form == 2;
         e->pmarch = form == 3;
+        e->qmarch = form == 4;
         if ((st = apply_march_shape(e, nts[a], k))) goto done;
-        if ((form == 1 && !e->tmarch) || (form == 2 && !e->amarch) || (form == 3 && !pmarch_fits(e)))
+        if ((form == 1 && !e->tmarch) || (form == 2 && !e->amarch) || (form == 3 && !pmarch_fits(e)) ||
+            (form == 4 && !e->qmarch))
           continue;  // the form cannot run this batch
         PassArgs pa = pass_args(e);
         pa.dir = d_dir;
@@ -1127,6 +1154,7 @@ extern "C" mcx_status mcx_autotune(mcx_engine *e, int *block, int *planes, float
   e->tmarch = best_form == 1;
   e->amarch = best_form == 2;
   e->pmarch = best_form == 3;
+  e->qmarch = best_form == 4;
   st = apply_march_shape(e, best_nt, best_k);
   if (st == MCX_OK) st = check_err_flag(e);
 done:

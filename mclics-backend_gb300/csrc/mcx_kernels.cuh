@@ -103,6 +103,11 @@ bool amarch_prepare(const Variant &v, int nt);
 int amarch_smem_bytes(int nt);
 int amarch_blocks_per_sm(const Variant &v, int nt);
 void launch_amarch(const Variant &v, int mode, const PassArgs &a, int nt, bool pdl, cudaStream_t st);
+// The z-march with four same-colour sites per thread (mcx_qmarch.cu;
+// unmasked batches, nx a multiple of 8): units of 2 x nt pairs.
+bool qmarch_prepare(const Variant &v, int nt);
+int qmarch_blocks_per_sm(const Variant &v, int nt);
+void launch_qmarch(const Variant &v, int mode, const PassArgs &a, int nt, bool pdl, cudaStream_t st);
 // The z-march as one cooperative launch for nsweeps sweeps (mcx_pmarch.cu):
 // a.units must fit one wave (pmarch_blocks_per_sm per SM); bar is a counter
 // the launch zeroes first; extra > 0 makes every grid barrier unreachable

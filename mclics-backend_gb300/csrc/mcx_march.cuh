@@ -15,8 +15,13 @@ namespace mcx {
 // that an SM's L1 still held from before the previous pass's writes (the
 // chain then differed from a launch-by-launch run), while L2 loads always
 // see them.
+#ifdef MCX_OPP_L1
+__device__ __forceinline__ float2 ldo2(const float *p) { return *reinterpret_cast<const float2 *>(p); }
+__device__ __forceinline__ float ldo1(const float *p) { return *p; }
+#else
 __device__ __forceinline__ float2 ldo2(const float *p) { return __ldcg(reinterpret_cast<const float2 *>(p)); }
 __device__ __forceinline__ float ldo1(const float *p) { return __ldcg(p); }
+#endif
 
 // Programmatic dependent launch: wait until the preceding grid on the stream
 // has completed and its memory is visible (returns at once when the launch

@@ -30,7 +30,8 @@ BOUNDS = {"free": 0, "periodic": 1}
 ANCHORINGS = {"homeotropic": 0, "fg": 1, "rp": 2, "strong": 3, "homeotropic_ghrl": 4, "fg_ghrl": 5, "rp_ghrl": 6,
               "strong_ghrl": 7}
 PROPOSALS = {"plain": 0, "vmf_mlp": 1}
-PASSES = {"march": 0, "direct": 1, "staged": 2, "march_tma": 3, "march_async": 4, "march_persistent": 5}
+PASSES = {"march": 0, "direct": 1, "staged": 2, "march_tma": 3, "march_async": 4, "march_persistent": 5,
+          "march_quad": 6}
 MLP_PARAMS = 6792
 SAMPLE_FLOATS = 24
 AUG_FLIP, AUG_ROTATE = 1, 2

@@ -269,12 +269,13 @@ def test_errors_are_status_codes():
 KERNELS = [("march", 128, 8), ("march", 64, 1), ("march", 256, 32), ("march", 128, 3), ("march", 128, 0),
            ("march", 64, -3), ("march_tma", 128, 8), ("march_tma", 256, 0), ("march_tma", 64, 3),
            ("march_async", 256, 0), ("march_async", 128, 5), ("march_async", 64, 1), ("march_async", 256, 32),
-           ("march_persistent", 256, 0), ("march_persistent", 128, 0), ("direct", 0, 0), ("staged", 0, 0)]
+           ("march_persistent", 256, 0), ("march_persistent", 128, 0), ("direct", 0, 0), ("staged", 0, 0),
+           ("march_quad", 128, 8), ("march_quad", 64, 0), ("march_quad", 256, 3), ("march_quad", 128, -2)]
 
 
 def _run_kernel(descs, setup, kind, block, planes, sweeps=19):
     with mcx.Engine(descs) as eng:
-        if kind in ("staged", "march_tma", "march_async"):
+        if kind in ("staged", "march_tma", "march_async", "march_quad"):
             try:
                 eng.pass_kind = kind  # not every batch fits these kernels
             except mcx.McxError:
