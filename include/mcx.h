@@ -333,6 +333,17 @@ mcx_status mcx_collect_samples(mcx_engine *eng, int n, unsigned int seed, int au
 mcx_status mcx_train_mlp(mcx_engine *eng, const mcx_train_config *cfg, float *loss);
 mcx_status mcx_mlp_grad(mcx_engine *eng, const float *samples, int n, float *grad, float *loss);
 
+/* The network set by mcx_set_mlp on n rows of its 19 inputs (host, n x 19
+ * floats: the six neighbours x+ x- y+ y- z+ z- then T) -> outputs (host,
+ * n x 4: mu, log kappa before its clamp), on the GPU; no counterpart in the
+ * reference.  path MCX_MLP_TCGEN05 runs it on the 5th-generation tensor cores
+ * (tcgen05.mma, FP32 accumulators in tensor memory, 128 rows per MMA tile);
+ * MCX_MLP_WARP_MMA with the warp-level mma.sync code of the learned passes.
+ * Both take BF16 inputs, weights and activations with FP32 accumulation and
+ * the same GELU arithmetic; they differ only in the order of the FP32 sums. */
+enum { MCX_MLP_WARP_MMA = 0, MCX_MLP_TCGEN05 = 1 };
+mcx_status mcx_mlp_forward(mcx_engine *eng, const float *inputs, int n, float *outputs, int path);
+
 /* The engine's CUDA stream (a cudaStream_t), for callers that record events
  * or order their own work against the engine's. */
 void *mcx_stream(mcx_engine *eng);

@@ -897,6 +897,8 @@ static mcx_status check_err_flag(mcx_engine *e) {
     CK(e, cudaMemset(e->d_err, 0, sizeof f));
     if (f & 2u)
       return fail(e, MCX_ERR_CUDA, "persistent z-march: a grid barrier was not reached in time; results are invalid");
+    if (f & 4u)
+      return fail(e, MCX_ERR_CUDA, "tensor-core network: an MMA did not complete in time; results are invalid");
     return fail(e, MCX_ERR_CUDA, "staged pass: a shared-memory tile copy did not complete in time; results are invalid");
   }
   return MCX_OK;
@@ -1347,6 +1349,30 @@ extern "C" mcx_status mcx_mlp_grad(mcx_engine *e, const float *samples, int n, f
   CK(e, cudaStreamSynchronize(e->stream));
   if (loss) *loss = l;
   return MCX_OK;
+}
+
+extern "C" mcx_status mcx_mlp_forward(mcx_engine *e, const float *inputs, int n, float *outputs, int path) {
+  if (!e) return fail(nullptr, MCX_ERR_INVALID, "null engine");
+  if (!inputs || !outputs || n < 1) return fail(e, MCX_ERR_INVALID, "mcx_mlp_forward: bad arguments");
+  if (path != MCX_MLP_WARP_MMA && path != MCX_MLP_TCGEN05)
+    return fail(e, MCX_ERR_INVALID, "mcx_mlp_forward: unknown path %d", path);
+  if (!e->d_mlp || e->mlp.empty()) return fail(e, MCX_ERR_INVALID, "mcx_mlp_forward: no network set (mcx_set_mlp)");
+  float *d_in = nullptr, *d_out = nullptr;
+  struct Bufs {
+    float **a, **b;
+    ~Bufs() {
+      cudaFree(*a);
+      cudaFree(*b);
+    }
+  } bufs{&d_in, &d_out};
+  CK(e, cudaMalloc(&d_in, sizeof(float) * 19 * (size_t)n));
+  CK(e, cudaMalloc(&d_out, sizeof(float) * 4 * (size_t)n));
+  CK(e, cudaMemcpyAsync(d_in, inputs, sizeof(float) * 19 * (size_t)n, cudaMemcpyHostToDevice, e->stream));
+  CK(e, launch_mlp_forward(e->d_mlp, d_in, n, d_out, path == MCX_MLP_TCGEN05, e->d_err, e->stream));
+  e->launches++;
+  CK(e, cudaMemcpyAsync(outputs, d_out, sizeof(float) * 4 * (size_t)n, cudaMemcpyDeviceToHost, e->stream));
+  CK(e, cudaStreamSynchronize(e->stream));
+  return check_err_flag(e);
 }
 
 extern "C" mcx_status mcx_train_mlp(mcx_engine *e, const mcx_train_config *cfg, float *loss) {

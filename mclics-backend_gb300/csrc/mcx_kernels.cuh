@@ -153,6 +153,12 @@ void launch_combine(const RepDev *rep, const RepState *st, const double *stats, 
 // Per-site local order parameter (natural order; NaN at inactive sites).
 void launch_local_order(const RepDev &R, const float *dir, const uint8_t *pt, float *out, cudaStream_t st);
 
+// The network on n rows of 19 inputs -> n x 4 outputs (mcx_tcmlp.cu): on the
+// tcgen05 tensor cores (accumulators in TMEM) or with the learned passes'
+// warp-level mma.sync code; err receives bit 4 when an MMA wait ran out.
+cudaError_t launch_mlp_forward(const uint8_t *mlp, const float *in, int n, float *out, int tensor_cores,
+                               unsigned *err, cudaStream_t st);
+
 // Training of the learned proposal's network (mcx_train.cu).
 int train_smem_bytes();
 int sample_floats();

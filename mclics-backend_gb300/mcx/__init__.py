@@ -171,6 +171,7 @@ def lib() -> C.CDLL:
         L.mcx_collect_samples.argtypes = [V, I, C.c_uint, I, V]
         L.mcx_train_mlp.argtypes = [V, C.POINTER(TrainConfig), V]
         L.mcx_mlp_grad.argtypes = [V, V, I, V, V]
+        L.mcx_mlp_forward.argtypes = [V, V, I, V, I]
         _lib = L
     return _lib
 
@@ -353,6 +354,15 @@ class Engine:
         loss = np.zeros(1, np.float32)
         self._ck(self._L.mcx_mlp_grad(self._h, _p(s), int(s.shape[0]), _p(g), _p(loss)))
         return float(loss[0]), g
+
+    def mlp_forward(self, inputs: np.ndarray, path: str = "tcgen05") -> np.ndarray:
+        """The network on rows of its 19 inputs -> [n, 4] outputs, on the
+        tcgen05 tensor cores ("tcgen05") or with the learned passes' warp-level
+        mma.sync code ("warp")."""
+        x = np.ascontiguousarray(inputs, np.float32).reshape(-1, 19)
+        y = np.zeros((x.shape[0], 4), np.float32)
+        self._ck(self._L.mcx_mlp_forward(self._h, _p(x), int(x.shape[0]), _p(y), {"warp": 0, "tcgen05": 1}[path]))
+        return y
 
     def polarization(self, r: int) -> float:
         P = C.c_double()

@@ -176,3 +176,31 @@ def test_learned_forms_agree_over_long_runs():
     for a, b in zip(*means):
         se = np.sqrt(a.var(ddof=1) / len(a) + b.var(ddof=1) / len(b))
         assert abs(a.mean() - b.mean()) <= 5 * se + 1e-6 * abs(a.mean()), (a.mean(), b.mean(), se)
+
+
+@pytest.mark.parametrize("n", [1, 5, 128, 1000, 40000])
+def test_network_on_tensor_cores_matches_the_oracle(n):
+    """mcx_mlp_forward: the network on the tcgen05 tensor cores (FP32
+    accumulators in tensor memory) and with the learned passes' warp-level
+    mma.sync code, on rows of neighbour directors (some absent) and
+    temperatures, against the FP64 forward pass with the engine's BF16
+    roundings (within 3e-2, as the learned pass's outputs); the two GPU paths
+    take the same BF16 operands and differ only in the order of the FP32 sums,
+    so they agree to 1e-2 on every output and exactly on most."""
+    params = _weights(11)
+    rng = np.random.default_rng(n)
+    nb = O.random_directors(6 * n, rng).reshape(n, 6, 3)
+    nb[rng.random((n, 6)) < 0.15] = 0.0
+    X = M.features(nb, rng.uniform(0.5, 1.5, n))
+    ref = M.forward_bf16(params, X)
+    m = O.Model(nx=8, ny=8, nz=8, potential="ll")
+    with mcx.Engine([desc_from_model(m)]) as eng:
+        eng.set_mlp(M.pack_weights(params))
+        tc = eng.mlp_forward(X, "tcgen05")
+        wp = eng.mlp_forward(X, "warp")
+        again = eng.mlp_forward(X, "tcgen05")
+    assert np.max(np.abs(tc - ref)) < 3e-2, np.max(np.abs(tc - ref))
+    assert np.max(np.abs(wp - ref)) < 3e-2, np.max(np.abs(wp - ref))
+    assert np.max(np.abs(tc - wp)) < 1e-2
+    assert np.mean(tc == wp) > 0.5
+    assert np.array_equal(tc, again)  # deterministic run to run
