@@ -343,6 +343,15 @@ mcx_status mcx_mlp_grad(mcx_engine *eng, const float *samples, int n, float *gra
  * the same GELU arithmetic; they differ only in the order of the FP32 sums. */
 enum { MCX_MLP_WARP_MMA = 0, MCX_MLP_TCGEN05 = 1 };
 mcx_status mcx_mlp_forward(mcx_engine *eng, const float *inputs, int n, float *outputs, int path);
+/* Which code evaluates the network inside the learned z-march (the learned
+ * proposal's sweep kernel): MCX_MLP_TCGEN05 evaluates each plane's 256 sites
+ * of a CTA as two M = 128 tcgen05 tiles with the accumulators in tensor
+ * memory; MCX_MLP_WARP_MMA, the default (measured faster), the warp-level
+ * mma.sync code.  Call after mcx_set_mlp.  The two give the same outputs up
+ * to the order of FP32 sums, so their chains part after a few sweeps but
+ * sample the same law.  No counterpart in the reference. */
+mcx_status mcx_set_mlp_path(mcx_engine *eng, int path);
+int mcx_get_mlp_path(const mcx_engine *eng);
 
 /* The engine's CUDA stream (a cudaStream_t), for callers that record events
  * or order their own work against the engine's. */

@@ -83,6 +83,7 @@ struct mcx_engine {
   std::vector<int4> lunits;
   int4 *d_lunits = nullptr;
   bool lmarch_ok = false;
+  bool ltc = false;  // the learned z-march's network on the tcgen05 tensor cores (else warp-level mma.sync)
   int tm_o = 0, tm_a = 0;  // its shared-memory slot sizes (floats)
   std::vector<int4> units;
   int4 *d_units = nullptr;
@@ -785,7 +786,7 @@ static void launch_sweep_pass(mcx_engine *e, PassArgs &pa, int colour, bool meas
     if (e->march && e->lmarch_ok) {
       pa.units = e->d_lunits;
       pa.nunits = (int)e->lunits.size();
-      launch_lmarch(e->var, mode, pa, e->pdl, e->stream);
+      launch_lmarch(e->var, mode, pa, e->pdl, e->ltc, e->stream);
     } else {
       launch_pass_learned(e->var, mode, pa, e->lgrid[mode], e->stream);
     }
@@ -1222,7 +1223,11 @@ static mcx_status upload_mlp(mcx_engine *e, const float *w) {
       e->lgrid[m] = (int)std::min<long long>((long long)per * nsm, (long long)e->map.size());
     }
     const char *lm = getenv("MCX_LMARCH");
-    e->lmarch_ok = !(lm && atoi(lm) == 0) && lmarch_prepare(e->var);
+    const char *lp = getenv("MCX_MLP_PATH");
+    // the warp-level network is the default: measured faster inside the
+    // learned z-march (LL 96^3 x 128: 3.43 against 3.87 ms per pass)
+    e->ltc = lp && atoi(lp) == MCX_MLP_TCGEN05 && lmarch_prepare(e->var, true);
+    e->lmarch_ok = !(lm && atoi(lm) == 0) && lmarch_prepare(e->var, e->ltc);
     if (e->lmarch_ok)
       if (mcx_status st = plan_lmarch(e)) return st;
   }
@@ -1350,6 +1355,23 @@ extern "C" mcx_status mcx_mlp_grad(mcx_engine *e, const float *samples, int n, f
   if (loss) *loss = l;
   return MCX_OK;
 }
+
+extern "C" mcx_status mcx_set_mlp_path(mcx_engine *e, int path) {
+  if (!e) return fail(nullptr, MCX_ERR_INVALID, "null engine");
+  if (path != MCX_MLP_WARP_MMA && path != MCX_MLP_TCGEN05)
+    return fail(e, MCX_ERR_INVALID, "mcx_set_mlp_path: unknown path %d", path);
+  if (!e->d_mlp) return fail(e, MCX_ERR_INVALID, "mcx_set_mlp_path: set the network weights (mcx_set_mlp) first");
+  if (!e->lmarch_ok) return fail(e, MCX_ERR_UNSUPPORTED, "mcx_set_mlp_path: the learned z-march does not run this batch");
+  CK(e, cudaStreamSynchronize(e->stream));
+  if (path == MCX_MLP_TCGEN05 && !lmarch_prepare(e->var, true))
+    return fail(e, MCX_ERR_UNSUPPORTED, "mcx_set_mlp_path: the tensor-core form cannot be resident");
+  e->ltc = path == MCX_MLP_TCGEN05;
+  if (!lmarch_prepare(e->var, e->ltc)) return fail(e, MCX_ERR_CUDA, "mcx_set_mlp_path: learned z-march set-up failed");
+  drop_graphs(e);
+  return MCX_OK;
+}
+
+extern "C" int mcx_get_mlp_path(const mcx_engine *e) { return e && e->ltc ? MCX_MLP_TCGEN05 : MCX_MLP_WARP_MMA; }
 
 extern "C" mcx_status mcx_mlp_forward(mcx_engine *e, const float *inputs, int n, float *outputs, int path) {
   if (!e) return fail(nullptr, MCX_ERR_INVALID, "null engine");

@@ -117,10 +117,11 @@ int pmarch_blocks_per_sm(const Variant &v, int nt);
 cudaError_t launch_pmarch(const Variant &v, int mode, const PassArgs &a, int nt, int nsweeps, unsigned *bar,
                           cudaStream_t st, unsigned extra = 0);
 // The learned-proposal z-march (mcx_lmarch.cu): units of lmarch_block_threads()
-// pairs; lmarch_prepare sets its shared memory and checks residency.
+// pairs; lmarch_prepare sets its shared memory and checks residency.  tc: the
+// network on the tcgen05 tensor cores (else the warp-level mma.sync code).
 int lmarch_block_threads();
-bool lmarch_prepare(const Variant &v);
-void launch_lmarch(const Variant &v, int mode, const PassArgs &a, bool pdl, cudaStream_t st);
+bool lmarch_prepare(const Variant &v, bool tc);
+void launch_lmarch(const Variant &v, int mode, const PassArgs &a, bool pdl, bool tc, cudaStream_t st);
 // The direct pass with the learned proposal (mcx_learned.cu).
 void launch_pass_learned(const Variant &v, int mode, const PassArgs &a, int nblocks, cudaStream_t st);
 int pass_learned_blocks_per_sm(const Variant &v, int mode);

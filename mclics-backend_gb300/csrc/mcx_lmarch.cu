@@ -14,6 +14,14 @@
 //             (weights and one input/output tile per warp), four CTAs of 128
 //             threads per SM at 128 registers.
 //
+//             With TC the network runs on the 5th-generation tensor cores
+//             instead (tc_mlp, mcx_tcmlp.cuh): per plane the CTA's 128
+//             threads store their two sites' input rows as two M = 128 tiles
+//             (thread t is row t of each: site A, site B), one thread issues
+//             the tcgen05.mma of each layer, the accumulators sit in 128 TMEM
+//             columns of the CTA and every thread reads back its own rows.
+//             63 KB of shared memory per CTA (three CTAs per SM).
+//
 // It computes what the learned direct pass (k_pass<LEARN>) computes: the
 // same rows reach the network, the same per-site Philox counters drive the
 // draws.  Results agree bit for bit except where a decision lies within an
@@ -24,26 +32,48 @@
 
 #include "mcx_march.cuh"
 #include "mcx_mlp.cuh"
+#include "mcx_tcmlp.cuh"
 
 namespace mcx {
 
 constexpr int kLPB = 128;  // threads per CTA (4 warps)
 constexpr int kLmarchSmem = kMlpBytes + (kLPB / 32) * (64 * kXs * 2 + 64 * 4 * 4);
+constexpr int kLmarchTcSmem = kTcWBytes + 2 * kTcXBytes + 2 * kTcHBytes + 64;
+constexpr uint32_t kLmarchTcCols = 128;  // two tiles of 64 FP32 accumulator columns
 #ifndef MCX_LMARCH_MIN_BLOCKS
 #define MCX_LMARCH_MIN_BLOCKS 4
 #endif
 
-template <int POT, bool MASK, bool FIELD, int MODE>
-__global__ void __launch_bounds__(kLPB, MCX_LMARCH_MIN_BLOCKS) k_lmarch(PassArgs a) {
+// the tensor-core form holds 63 KB of shared memory: three CTAs per SM, so
+// each thread may use up to 170 registers
+template <int POT, bool MASK, bool FIELD, int MODE, bool TC>
+__global__ void __launch_bounds__(kLPB, TC ? 3 : MCX_LMARCH_MIN_BLOCKS) k_lmarch(PassArgs a) {
   static_assert(MODE == MODE_SWEEP || MODE == MODE_SWEEP_MEASURE, "sweep modes only");
-  extern __shared__ __align__(16) uint8_t dyn[];
+  extern __shared__ __align__(1024) uint8_t dyn[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   uint8_t *W = dyn;
   __nv_bfloat16 *X = reinterpret_cast<__nv_bfloat16 *>(dyn + kMlpBytes) + (size_t)warp * 64 * kXs;
   float *Y = reinterpret_cast<float *>(dyn + kMlpBytes + (kLPB / 32) * 64 * kXs * 2) + (size_t)warp * 64 * 4;
+  // tensor-core form: network image, two input tiles, two activation tiles,
+  // the MMA mbarrier and the TMEM address
+  uint8_t *TX = dyn + kTcWBytes, *TH = TX + 2 * kTcXBytes;
+  uint64_t *tbar = reinterpret_cast<uint64_t *>(TH + 2 * kTcHBytes);
+  uint32_t *tslot = reinterpret_cast<uint32_t *>(tbar + 1);
+  uint32_t tmem = 0, tphase = 0;
   // the weights are written only between launches (host copies on the stream)
-  for (int i = threadIdx.x; i < kMlpBytes / 16; i += kLPB)
-    reinterpret_cast<int4 *>(W)[i] = reinterpret_cast<const int4 *>(a.mlp)[i];
+  if (TC) {
+    tc_load_weights(a.mlp, W, kLPB);
+    if (threadIdx.x == 0) {
+      mbar_init(tbar, 1);
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) tc_alloc(tslot, kLmarchTcCols);
+    fence_proxy_async();
+    tc_fence_before();
+  } else {
+    for (int i = threadIdx.x; i < kMlpBytes / 16; i += kLPB)
+      reinterpret_cast<int4 *>(W)[i] = reinterpret_cast<const int4 *>(a.mlp)[i];
+  }
   const int4 u = a.units[blockIdx.x];
   const int r = u.x, c = a.colour;
   const RepDev &R = a.reps[r];
@@ -61,6 +91,10 @@ __global__ void __launch_bounds__(kLPB, MCX_LMARCH_MIN_BLOCKS) k_lmarch(PassArgs
 #pragma unroll
   for (int q = 0; q < kQ; q++) qs[q] = 0.f;
   __syncthreads();  // weights in shared memory
+  if (TC) {
+    tc_fence_after();
+    tmem = *tslot;
+  }
   grid_dependency_wait(m);
   if (MASK && (u.w & kUnitDead)) {  // no active site in or next to the unit: field energies only
     if (valid) dead_unit<FIELD, MODE>(R, m, kb, ke, qs);
@@ -130,20 +164,38 @@ __global__ void __launch_bounds__(kLPB, MCX_LMARCH_MIN_BLOCKS) k_lmarch(PassArgs
       wB[2 + q] = wt(erz[q], MASK ? (uint8_t)(o.pt >> 8) : 1);
     }
     const int psA = MASK ? (pself & 0xFF) : 1, psB = MASK ? (pself >> 8) : 1;
-    // the network for the warp's 64 sites
-    __syncwarp();
-    write_features(X + (size_t)(2 * lane) * kXs, nbA, wA, T, valid);
-    write_features(X + (size_t)(2 * lane + 1) * kXs, nbB, wB, T, valid && m.hasB);
-    __syncwarp();
-    mlp_warp(W, X, Y);
-    __syncwarp();
-    if (valid) {
-      float yA[4], yB[4];
+    float yA[4], yB[4];
+    if (TC) {
+      // the network for the CTA's 256 sites: two M = 128 tiles on the tensor cores
+      uint32_t fw[16];
+      feature_words(nbA, wA, T, valid, fw);
+      tc_store_row32(TX, threadIdx.x, fw);
+      feature_words(nbB, wB, T, valid && m.hasB, fw);
+      tc_store_row32(TX + kTcXBytes, threadIdx.x, fw);
+      fence_proxy_async();
+      __syncthreads();
+      float y[2][4];
+      if (!tc_mlp(W, TX, TH, 2, tmem, tbar, tphase, y, a.err)) break;  // uniform: every thread saw the same waits
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        yA[q] = y[0][q];
+        yB[q] = y[1][q];
+      }
+    } else {
+      // the network for the warp's 64 sites
+      __syncwarp();
+      write_features(X + (size_t)(2 * lane) * kXs, nbA, wA, T, valid);
+      write_features(X + (size_t)(2 * lane + 1) * kXs, nbB, wB, T, valid && m.hasB);
+      __syncwarp();
+      mlp_warp(W, X, Y);
+      __syncwarp();
 #pragma unroll
       for (int q = 0; q < 4; q++) {
         yA[q] = Y[(2 * lane) * 4 + q];
         yB[q] = Y[(2 * lane + 1) * 4 + q];
       }
+    }
+    if (valid) {
       // odd nx: the phantom in the last slot of an s = 1 row is skipped
       const bool skipA = MASK && s == 1 && m.tail == 1, skipB = MASK && s == 1 && m.tail == 2;
       if (!skipA) {
@@ -186,53 +238,65 @@ __global__ void __launch_bounds__(kLPB, MCX_LMARCH_MIN_BLOCKS) k_lmarch(PassArgs
   }
   grid_launch_dependents();
   flush_replica<kLPB, MODE>(a, r, 1, (unsigned)R.lcta, acc, qs, MASK);
-}
-
-template <int POT, bool MASK, bool FIELD>
-static const void *lmarch_fn(int mode) {
-  return mode == MODE_SWEEP_MEASURE ? (const void *)k_lmarch<POT, MASK, FIELD, MODE_SWEEP_MEASURE>
-                                    : (const void *)k_lmarch<POT, MASK, FIELD, MODE_SWEEP>;
-}
-
-static const void *lmarch_kernel(const Variant &v, int mode) {
-  if (v.pot == POT_LL) {
-    if (v.mask) return v.field ? lmarch_fn<POT_LL, true, true>(mode) : lmarch_fn<POT_LL, true, false>(mode);
-    return v.field ? lmarch_fn<POT_LL, false, true>(mode) : lmarch_fn<POT_LL, false, false>(mode);
+  if (TC) {  // every TMEM read is done (tc_mlp ends on a fenced barrier; flush_replica syncs again)
+    tc_fence_after();
+    if (warp == 0) tc_dealloc(tmem, kLmarchTcCols);
   }
-  if (v.mask) return v.field ? lmarch_fn<POT_GHRL, true, true>(mode) : lmarch_fn<POT_GHRL, true, false>(mode);
-  return v.field ? lmarch_fn<POT_GHRL, false, true>(mode) : lmarch_fn<POT_GHRL, false, false>(mode);
 }
+
+template <int POT, bool MASK, bool FIELD, bool TC>
+static const void *lmarch_fn(int mode) {
+  return mode == MODE_SWEEP_MEASURE ? (const void *)k_lmarch<POT, MASK, FIELD, MODE_SWEEP_MEASURE, TC>
+                                    : (const void *)k_lmarch<POT, MASK, FIELD, MODE_SWEEP, TC>;
+}
+
+template <bool TC>
+static const void *lmarch_kernel_tc(const Variant &v, int mode) {
+  if (v.pot == POT_LL) {
+    if (v.mask) return v.field ? lmarch_fn<POT_LL, true, true, TC>(mode) : lmarch_fn<POT_LL, true, false, TC>(mode);
+    return v.field ? lmarch_fn<POT_LL, false, true, TC>(mode) : lmarch_fn<POT_LL, false, false, TC>(mode);
+  }
+  if (v.mask) return v.field ? lmarch_fn<POT_GHRL, true, true, TC>(mode) : lmarch_fn<POT_GHRL, true, false, TC>(mode);
+  return v.field ? lmarch_fn<POT_GHRL, false, true, TC>(mode) : lmarch_fn<POT_GHRL, false, false, TC>(mode);
+}
+
+static const void *lmarch_kernel(const Variant &v, int mode, bool tc) {
+  return tc ? lmarch_kernel_tc<true>(v, mode) : lmarch_kernel_tc<false>(v, mode);
+}
+
+static int lmarch_smem(bool tc) { return tc ? kLmarchTcSmem : kLmarchSmem; }
 
 int lmarch_block_threads() { return kLPB; }
 
-bool lmarch_prepare(const Variant &v) {
+bool lmarch_prepare(const Variant &v, bool tc) {
   if (v.pot == POT_PEAR) return false;
   for (int mode : {MODE_SWEEP, MODE_SWEEP_MEASURE})
-    if (cudaFuncSetAttribute(lmarch_kernel(v, mode), cudaFuncAttributeMaxDynamicSharedMemorySize, kLmarchSmem) !=
-        cudaSuccess)
+    if (cudaFuncSetAttribute(lmarch_kernel(v, mode, tc), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             lmarch_smem(tc)) != cudaSuccess)
       return false;
   int n = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, lmarch_kernel(v, MODE_SWEEP), kLPB, kLmarchSmem) !=
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, lmarch_kernel(v, MODE_SWEEP, tc), kLPB, lmarch_smem(tc)) !=
       cudaSuccess)
     return false;
-  return n > 0;
+  // the tensor-core form's CTAs must all find their TMEM columns (512 per SM)
+  return n > 0 && (!tc || (uint32_t)n * kLmarchTcCols <= 512);
 }
 
-void launch_lmarch(const Variant &v, int mode, const PassArgs &a, bool pdl, cudaStream_t st) {
+void launch_lmarch(const Variant &v, int mode, const PassArgs &a, bool pdl, bool tc, cudaStream_t st) {
   if (v.pot == POT_PEAR) return;  // the learned proposal is refused for Pear
   PassArgs args = a;
   void *params[] = {&args};
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(a.nunits);
   cfg.blockDim = dim3(kLPB);
-  cfg.dynamicSmemBytes = kLmarchSmem;
+  cfg.dynamicSmemBytes = lmarch_smem(tc);
   cfg.stream = st;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
   attr[0].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = attr;
   cfg.numAttrs = pdl ? 1 : 0;
-  cudaLaunchKernelExC(&cfg, lmarch_kernel(v, mode), params);
+  cudaLaunchKernelExC(&cfg, lmarch_kernel(v, mode, tc), params);
 }
 
 }  // namespace mcx

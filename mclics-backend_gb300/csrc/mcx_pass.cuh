@@ -616,10 +616,10 @@ __device__ __forceinline__ unsigned site_update_learned(const RepDev &R, const P
 }
 
 // Network input row of one site: its six neighbours (absent or inactive ones
-// as zero vectors) in slot order, then T, then zeros to 32 columns; BF16.
-__device__ __forceinline__ void write_features(__nv_bfloat16 *row, const float nb[6][3], const float w[6], float T,
-                                               bool live) {
-  uint32_t *r = reinterpret_cast<uint32_t *>(row);
+// as zero vectors) in slot order, then T, then zeros to 32 columns; BF16,
+// packed in pairs.
+__device__ __forceinline__ void feature_words(const float nb[6][3], const float w[6], float T, bool live,
+                                              uint32_t r[16]) {
   float f[20];
 #pragma unroll
   for (int d = 0; d < 6; d++) {
@@ -634,6 +634,15 @@ __device__ __forceinline__ void write_features(__nv_bfloat16 *row, const float n
   for (int q = 0; q < 10; q++) r[q] = pack_bf16(f[2 * q], f[2 * q + 1]);
 #pragma unroll
   for (int q = 10; q < 16; q++) r[q] = 0u;
+}
+
+__device__ __forceinline__ void write_features(__nv_bfloat16 *row, const float nb[6][3], const float w[6], float T,
+                                               bool live) {
+  uint32_t r[16];
+  feature_words(nb, w, T, live, r);
+  uint32_t *d = reinterpret_cast<uint32_t *>(row);
+#pragma unroll
+  for (int q = 0; q < 16; q++) d[q] = r[q];
 }
 
 template <int POT, bool MASK, bool FIELD, int MODE>

@@ -172,6 +172,9 @@ def lib() -> C.CDLL:
         L.mcx_train_mlp.argtypes = [V, C.POINTER(TrainConfig), V]
         L.mcx_mlp_grad.argtypes = [V, V, I, V, V]
         L.mcx_mlp_forward.argtypes = [V, V, I, V, I]
+        L.mcx_set_mlp_path.argtypes = [V, I]
+        L.mcx_get_mlp_path.argtypes = [V]
+        L.mcx_get_mlp_path.restype = I
         _lib = L
     return _lib
 
@@ -363,6 +366,15 @@ class Engine:
         y = np.zeros((x.shape[0], 4), np.float32)
         self._ck(self._L.mcx_mlp_forward(self._h, _p(x), int(x.shape[0]), _p(y), {"warp": 0, "tcgen05": 1}[path]))
         return y
+
+    @property
+    def mlp_path(self) -> str:
+        """The learned z-march's network code: "tcgen05" or "warp"."""
+        return "tcgen05" if self._L.mcx_get_mlp_path(self._h) == 1 else "warp"
+
+    @mlp_path.setter
+    def mlp_path(self, path: str):
+        self._ck(self._L.mcx_set_mlp_path(self._h, {"warp": 0, "tcgen05": 1}[path]))
 
     def polarization(self, r: int) -> float:
         P = C.c_double()

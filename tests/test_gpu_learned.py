@@ -90,11 +90,13 @@ def test_learned_pass_parity(name):
             assert np.array_equal(after, want)
 
 
+@pytest.mark.parametrize("path", ["tcgen05", "warp"])
 @pytest.mark.parametrize("T", [0.8, 1.6])
-def test_learned_chain_samples_the_same_equilibrium(T):
+def test_learned_chain_samples_the_same_equilibrium(T, path):
     """Random (untrained) weights: a poor proposal, but the exact MH ratio
     keeps the Boltzmann distribution -- E and S agree with the plain chain
-    within 3 combined standard errors over 32 replicas each."""
+    within 3 combined standard errors over 32 replicas each, with the learned
+    z-march's network on the tensor cores or at warp level."""
     m = O.Model(nx=8, ny=8, nz=8, potential="ll")
     params = _weights(2, scale=1.0)
     R = 32
@@ -106,6 +108,7 @@ def test_learned_chain_samples_the_same_equilibrium(T):
                 eng.init_random(r, 7 + r)
             if kind == "vmf_mlp":
                 eng.set_mlp(M.pack_weights(params))
+                eng.mlp_path = path
                 eng.set_proposal("vmf_mlp")
             eng.sweep(600)
             eng.reset_stats()
@@ -128,8 +131,9 @@ IDENTITY_CASES = {**CASES,
 
 @pytest.mark.parametrize("name", list(IDENTITY_CASES))
 def test_learned_march_equals_learned_direct_pass(name):
-    """The learned z-march and the learned direct pass give bit-identical
-    states, step sizes and acceptance counts after measured sweeps."""
+    """The learned z-march with the warp-level network and the learned direct
+    pass give bit-identical states, step sizes and acceptance counts after
+    measured sweeps."""
     m = IDENTITY_CASES[name]
     params = _weights(4)
     lat = O.Lattice(m)
@@ -139,6 +143,9 @@ def test_learned_march_equals_learned_direct_pass(name):
             eng.pass_kind = kind
             eng.set_state(0, random_state(m, lat.pt, np.random.default_rng(6)))
             eng.set_mlp(M.pack_weights(params))
+            if kind == "march":
+                eng.mlp_path = "warp"
+                assert eng.mlp_path == "warp"
             eng.set_proposal("vmf_mlp")
             eng.sweep(11, measure=True)
             out.append((eng.get_state(0), eng.stats(0)))
@@ -149,33 +156,38 @@ def test_learned_march_equals_learned_direct_pass(name):
 
 
 def test_learned_forms_agree_over_long_runs():
-    """16 chiral droplets in a field, 50 + 50 measured learned sweeps: the
-    learned z-march and the learned direct pass may part after a decision
-    within an ulp of its threshold (their multiply-adds are fused by the
-    compiler in each kernel), but they sample the same states: replica-averaged
-    S and E agree within their statistical error."""
+    """32 chiral droplets in a field, 50 + 50 measured learned sweeps: the
+    learned z-march with the tensor-core network, with the warp-level network,
+    and the learned direct pass part (the tensor-core network sums in another
+    order; decisions within an ulp of their threshold part the other two),
+    but they sample the same states: replica-averaged S and E of each z-march
+    form agree with the direct pass's within 3 combined standard errors."""
     m = O.Model(nx=64, ny=64, nz=64, geometry="sphere", xbound="free", ybound="free", zbound="free",
                 potential="ghrl", k11=1.0, k22=0.6, k33=1.4, p0=20.0, elecA=1.0, elecZ=1.0, elecE=0.5, radius=26.0,
                 surfaces=[O.Surface("fg", 1.0)])
-    descs = [desc_from_model(m, T=0.8, seed=500 + q, stream=q) for q in range(16)]
+    R = 32
+    descs = [desc_from_model(m, T=0.8, seed=500 + q, stream=q) for q in range(R)]
     params = _weights(4)
     means = []
-    for kind in ("march", "direct"):
+    for kind, path in (("direct", None), ("march", "tcgen05"), ("march", "warp")):
         with mcx.Engine(descs) as eng:
             eng.pass_kind = kind
-            for q in range(16):
+            for q in range(R):
                 eng.init_random(q, 11 + q)
             eng.set_mlp(M.pack_weights(params))
+            if path:
+                eng.mlp_path = path
             eng.set_proposal("vmf_mlp")
             eng.sweep(50)
             eng.reset_stats()
             eng.sweep(50, measure=True)
-            st = [eng.stats(q) for q in range(16)]
+            st = [eng.stats(q) for q in range(R)]
         means.append((np.array([t[mcx.ST_S1] / t[mcx.ST_N] for t in st]),
                       np.array([t[mcx.ST_E1] / t[mcx.ST_N] for t in st])))
-    for a, b in zip(*means):
-        se = np.sqrt(a.var(ddof=1) / len(a) + b.var(ddof=1) / len(b))
-        assert abs(a.mean() - b.mean()) <= 5 * se + 1e-6 * abs(a.mean()), (a.mean(), b.mean(), se)
+    for other in means[1:]:
+        for a, b in zip(means[0], other):
+            se = np.sqrt(a.var(ddof=1) / len(a) + b.var(ddof=1) / len(b))
+            assert abs(a.mean() - b.mean()) <= 3 * se, (a.mean(), b.mean(), se)
 
 
 @pytest.mark.parametrize("n", [1, 5, 128, 1000, 40000])
