@@ -599,3 +599,43 @@ def test_pass_forms_part_only_at_near_ties():
             pa = np.exp(-d64 / T)
             assert abs(u[2] - pa) <= TIE * (1 + pa), (int(s), u[2], pa, d64)
     print(f"parted at sweep {n} in replica {q}: {len(differ)} sites differ, {flips} near-tie decisions of colour {c}")
+
+
+OBS_CASES = {
+    "ll_bulk_48": O.Model(nx=48, ny=48, nz=48, potential="ll"),
+    "ghrl_slab_32_field": O.Model(nx=32, ny=32, nz=32, geometry="slab", potential="ghrl", k11=1.0, k22=0.8, k33=1.2,
+                                  elecA=0.5, elecZ=1.0, elecE=1.0,
+                                  surfaces=[O.Surface("homeotropic", 4.0), O.Surface("homeotropic", 4.0)]),
+    "ghrl_sphere_33_chiral": O.Model(nx=33, ny=33, nz=33, geometry="sphere", potential="ghrl", k11=1.0, k22=0.6,
+                                     k33=1.4, p0=20, elecA=1.0, elecZ=1.0, elecE=1.5,
+                                     surfaces=[O.Surface("fg", 1.0)]),
+}
+
+
+@pytest.mark.parametrize("ordered", [False, True], ids=["random", "ordered"])
+@pytest.mark.parametrize("name", list(OBS_CASES))
+def test_observable_errors_against_fp64(name, ordered):
+    """The measured error of E, E_valid, Q and S of the GPU's measurement
+    (FP32 sums per CTA, FP64 across CTAs, FP64 Jacobi) against the oracle's
+    FP64 re-evaluation of the same directors, printed (OBSERVABLE_ERRORS) and
+    bounded: relative 2e-6 for E and E_valid, absolute 2e-6 for Q and S."""
+    import json
+    m = OBS_CASES[name]
+    lat = O.Lattice(m)
+    rng = np.random.default_rng(5)
+    ni = random_state(m, lat.pt, rng)
+    if ordered:  # a nematic state near S = 0.8
+        ni = ni * 0.35 + np.array([0.1, 0.2, 0.95], np.float32)
+        ni /= np.linalg.norm(ni, axis=1, keepdims=True)
+        ni[lat.pt == 0] = (0, 0, 1)
+    with mcx.Engine([desc_from_model(m)]) as eng:
+        eng.set_state(0, ni)
+        g = eng.measure(0)
+    lat.ni[:] = ni
+    o = lat.measure()
+    err = {"case": name + ("_ordered" if ordered else "_random"), "S": float(o["S"]),
+           "E_rel": abs(g["E"] - o["E"]) / abs(o["E"]), "E_valid_rel": abs(g["E_valid"] - o["E_valid"]) / abs(o["E_valid"]),
+           "Q_abs": float(np.max(np.abs(np.asarray(g["Q"]) - o["Q"]))), "S_abs": abs(g["S"] - o["S"])}
+    print("OBSERVABLE_ERRORS " + json.dumps(err))
+    assert err["E_rel"] < 2e-6 and err["E_valid_rel"] < 2e-6
+    assert err["Q_abs"] < 2e-6 and err["S_abs"] < 2e-6
