@@ -139,6 +139,19 @@ __host__ __device__ __forceinline__ void pair_uniforms(uint4 w, float uA[3], flo
 
 // Chiral term component as the reference writes it (src/potential.cpp:30-32)
 // for r = +e_axis: (a x b) with the reference's sign convention.
+// a . b with its roundings fixed (this order; fmaf is always fused)
+__device__ __forceinline__ float dot3_rn(float ax, float ay, float az, float bx, float by, float bz) {
+  return fmaf(az, bz, fmaf(ay, by, __fmul_rn(ax, bx)));
+}
+
+// cross_ref with its roundings fixed
+template <int AXIS>
+__device__ __forceinline__ float cross_ref_rn(float ax, float ay, float az, float bx, float by, float bz) {
+  if (AXIS == 0) return fmaf(az, by, -__fmul_rn(ay, bz));
+  if (AXIS == 1) return fmaf(ax, bz, -__fmul_rn(az, bx));
+  return fmaf(ay, bx, -__fmul_rn(ax, by));
+}
+
 template <int AXIS>
 __device__ __forceinline__ float cross_ref(float ax, float ay, float az, float bx, float by, float bz) {
   if (AXIS == 0) return az * by - ay * bz;
@@ -172,13 +185,15 @@ __device__ __forceinline__ float ghrl_bond_var(const RepDev &R, float ax, float 
                                                float bz, float sign) {
   const float ai = AXIS == 0 ? ax : (AXIS == 1 ? ay : az);
   const float aj = AXIS == 0 ? bx : (AXIS == 1 ? by : bz);
-  const float nij = ax * bx + ay * by + az * bz;
-  const float q = nij * nij;
-  const float E1 = 1.5f * ai * ai + (1.5f * aj * aj - 1.0f);
-  float v = E1 * (R.ga * q + R.gb) + R.gc * q + (R.mu * aj) * (ai * nij);
+  // roundings fixed (explicit intrinsics): the pass's energy changes are
+  // the same bits in every kernel
+  const float nij = dot3_rn(ax, ay, az, bx, by, bz);
+  const float q = __fmul_rn(nij, nij);
+  const float E1 = fmaf(__fmul_rn(1.5f, ai), ai, fmaf(__fmul_rn(1.5f, aj), aj, -1.0f));
+  float v = fmaf(E1, fmaf(R.ga, q, R.gb), fmaf(R.gc, q, __fmul_rn(__fmul_rn(R.mu, aj), __fmul_rn(ai, nij))));
   if (R.sigma != 0.f) {  // the chiral term (p0 != 0); the branch is uniform: a CTA serves one replica
-    const float cr = sign * cross_ref<AXIS>(ax, ay, az, bx, by, bz);
-    v += R.sigma * (nij > 0.f ? cr : -cr);
+    const float cr = sign * cross_ref_rn<AXIS>(ax, ay, az, bx, by, bz);  // sign is +-1: exact
+    v = fmaf(R.sigma, nij > 0.f ? cr : -cr, v);
   }
   return v;
 }
@@ -240,8 +255,8 @@ static __device__ __noinline__ float surface_energy(const RepDev &R, int sid, fl
 
 // Electric term (src/potential.cpp:39-43).
 __device__ __forceinline__ float field_energy(const RepDev &R, float nx, float ny, float nz) {
-  const float d = R.elecE * (nx * R.ex + ny * R.ey + nz * R.ez);
-  return -R.elecA * d * d;
+  const float d = __fmul_rn(R.elecE, dot3_rn(nx, ny, nz, R.ex, R.ey, R.ez));
+  return __fmul_rn(__fmul_rn(-R.elecA, d), d);
 }
 
 }  // namespace mcx

@@ -31,19 +31,29 @@ constexpr int kPB = 128;
 namespace mcx {
 
 // Bond energy of director a with neighbour b in slot d (x+, x-, y+, y-, z+, z-).
+//
+// The energy change of a move fixes every rounding: a product that feeds a
+// sum is either an fmaf or an explicit __fmul_rn, which the compiler cannot
+// fuse with what follows, and sums keep their written order.  Every kernel
+// that inlines the update (each pass form) therefore computes the same bits
+// and takes the same Metropolis decisions; left to the compiler, two forms'
+// multiply-add fusions could differ and a decision within an ulp of its
+// threshold could go either way.  Products by 0/1 weights or by +-1 are
+// exact and stay plain, so the compiler can still fold them.
 template <int POT, int D>
 __device__ __forceinline__ float bond(const RepDev &R, float ax, float ay, float az, const float b[3]) {
+  const float nij = dot3_rn(ax, ay, az, b[0], b[1], b[2]);
   if (POT == POT_LL) {
-    const float nij = ax * b[0] + ay * b[1] + az * b[2];
-    return -1.5f * R.A * nij * nij;
+    return __fmul_rn(__fmul_rn(-1.5f, R.A), __fmul_rn(nij, nij));
   } else if (POT == POT_PEAR) {
     // src/potential.cpp:10-15: -A nij^2 - B1 nij - (C/4)(1 + 2 nij + nij^2)((nj - ni) . rij),
     // rij = +-(unit vector of the slot's axis)
-    const float nij = ax * b[0] + ay * b[1] + az * b[2];
     constexpr int X = D >> 1;
-    const float d = (X == 0 ? b[0] - ax : (X == 1 ? b[1] - ay : b[2] - az)) * ((D & 1) ? -1.f : 1.f);
-    const float splay = (1.f + 2.f * nij + nij * nij) * d;
-    return -R.A * nij * nij - R.B1 * nij - (R.C * 0.25f) * splay;
+    const float ai = X == 0 ? ax : (X == 1 ? ay : az);
+    const float aj = X == 0 ? b[0] : (X == 1 ? b[1] : b[2]);
+    const float d = (D & 1) ? __fsub_rn(ai, aj) : __fsub_rn(aj, ai);
+    const float splay = __fmul_rn(fmaf(nij, __fadd_rn(nij, 2.f), 1.f), d);
+    return fmaf(-R.A, __fmul_rn(nij, nij), fmaf(-R.B1, nij, __fmul_rn(-0.25f * R.C, splay)));
   } else {
     return ghrl_bond_var<(D >> 1)>(R, ax, ay, az, b[0], b[1], b[2], (D & 1) ? -1.f : 1.f);
   }
@@ -58,13 +68,12 @@ __device__ __forceinline__ float bond_sum(const RepDev &R, float ax, float ay, f
     float acc = 0.f;
 #pragma unroll
     for (int d = 0; d < 6; d++) {
-      const float nij = ax * nb[d][0] + ay * nb[d][1] + az * nb[d][2];
-      acc = fmaf(nij * w[d], nij, acc);
+      const float nij = dot3_rn(ax, ay, az, nb[d][0], nb[d][1], nb[d][2]);
+      acc = fmaf(nij * w[d], nij, acc);  // w is 0 or 1: nij * w is exact
     }
     return acc;
   } else {
-    float acc = 0.f;
-    acc = fmaf(w[0], bond<POT, 0>(R, ax, ay, az, nb[0]), acc);
+    float acc = w[0] * bond<POT, 0>(R, ax, ay, az, nb[0]);  // w is 0 or 1: exact
     acc = fmaf(w[1], bond<POT, 1>(R, ax, ay, az, nb[1]), acc);
     acc = fmaf(w[2], bond<POT, 2>(R, ax, ay, az, nb[2]), acc);
     acc = fmaf(w[3], bond<POT, 3>(R, ax, ay, az, nb[3]), acc);
@@ -92,7 +101,12 @@ __device__ __forceinline__ float bond_const(const RepDev &R, const float w[6]) {
 // as one rotation of the component pair (u, v) = (y, z), (z, x) or (x, y):
 // u' = u c + v s, v' = v c - u s, which is the reference's three formulas.
 // sin and cos are taken of |angle| and the sign restored, so a move and its
-// reverse are exact mirror images (a symmetric proposal).
+// reverse are exact mirror images (a symmetric proposal).  The rotation is
+// left to the compiler's multiply-add fusion (written with explicit fmaf it
+// costs 8% more instructions per pass); unlike the energy change, where a
+// difference only shows at a near tie, a form whose fusion differed here
+// would move every accepted site by an ulp, which the bit-for-bit tests
+// across forms see at once.
 __device__ __forceinline__ void propose(float x, float y, float z, float u0, float u1, float ang, float &px, float &py,
                                         float &pz) {
   const float va = (2.f * u0 - 1.f) * ang;
@@ -137,11 +151,15 @@ __device__ __forceinline__ unsigned site_update(const RepDev &R, const PassArgs 
       float px, py, pz;
       propose(x, y, z, u[0], u[1], ang, px, py, pz);
       const float b_new = bond_sum<POT>(R, px, py, pz, nb, w);
-      float dE = bond_scale<POT>(R) * (b_new - b_old);
-      if (surf) dE += surface_energy(R, sid, px, py, pz, sx, sy, sz) - surface_energy(R, sid, x, y, z, sx, sy, sz);
-      if (FIELD) dE += field_energy(R, px, py, pz) - field_energy(R, x, y, z);
+      // every rounding of dE is explicit (see bond()): all pass forms take
+      // the same decisions
+      float dE = __fmul_rn(bond_scale<POT>(R), __fsub_rn(b_new, b_old));
+      if (surf)
+        dE = __fadd_rn(dE, __fsub_rn(surface_energy(R, sid, px, py, pz, sx, sy, sz),
+                                     surface_energy(R, sid, x, y, z, sx, sy, sz)));
+      if (FIELD) dE = __fadd_rn(dE, __fsub_rn(field_energy(R, px, py, pz), field_energy(R, x, y, z)));
       // src/evolve.cpp:160: accept when u < exp(-(E_new - E_old)/T)
-      const bool accept = u[2] < __expf(-dE * invT);
+      const bool accept = u[2] < __expf(__fmul_rn(-dE, invT));
       if (TRACE) {
         a.tr_dE[nat] = dE;
         a.tr_acc[nat] = accept ? 1 : 0;
