@@ -364,6 +364,41 @@ def eigmax(Q) -> tuple:
     return lam, v
 
 
+def local_order(ni: np.ndarray, pt: np.ndarray, m: Model) -> np.ndarray:
+    """The local order parameter of the reference's snapshots
+    (lattice_order_parameter, src/parameter_order.cpp:62-113) at every site:
+    Q = sum (3 n n^T - I) / (2 points) over the site and its six neighbours
+    that exist (bounds) and are active, largest eigenvalue; FP64.  NaN at
+    inactive sites (the reference evaluates only active ones)."""
+    nx, ny, nz = m.nx, m.ny, m.nz
+    N = [nx, ny, nz]
+    B = list(m.effective_bounds())
+    out = np.full(m.n, np.nan)
+    for s in np.nonzero(pt)[0]:
+        i, j, k = s % nx, (s // nx) % ny, s // (nx * ny)
+        Q = np.zeros((3, 3))
+        pts = 0
+        for d in ((0, 0, 0), (-1, 0, 0), (1, 0, 0), (0, -1, 0), (0, 1, 0), (0, 0, -1), (0, 0, 1)):
+            c = [i + d[0], j + d[1], k + d[2]]
+            ok = True
+            for ax in range(3):
+                if c[ax] < 0 or c[ax] >= N[ax]:
+                    if B[ax] == "periodic":
+                        c[ax] %= N[ax]
+                    else:
+                        ok = False
+            if not ok:
+                continue
+            t = c[0] + nx * (c[1] + ny * c[2])
+            if pt[t] == 0:
+                continue
+            n = ni[t].astype(np.float64)
+            Q += 3 * np.outer(n, n) - np.eye(3)
+            pts += 1
+        out[s] = np.linalg.eigvalsh(Q / (2 * pts))[-1]
+    return out
+
+
 def random_directors(n: int, rng: np.random.Generator) -> np.ndarray:
     """Uniform on the sphere (z uniform in [-1,1], azimuth uniform)."""
     z = rng.uniform(-1, 1, n)

@@ -13,6 +13,7 @@
  * supports one lattice: callers load this library in a fresh process per
  * configuration.
  */
+#include <math.h>
 #include <omp.h>
 #include <stdio.h>
 #include <stdlib.h>
@@ -227,6 +228,18 @@ extern "C" float ref_energy(const float *ni) {
 extern "C" float ref_order(const float *ni, float Q[9], float vec[3]) {
   Matrice_constructor((float *)ni, Q, PT, *P);
   return Eigen_value_evaluation(Q, vec);
+}
+
+/* lattice_order_parameter (src/parameter_order.cpp:62-113) at every active
+ * site, the local S of the reference's snapshots; NaN at inactive sites. */
+extern "C" void ref_local_order(const float *ni, float *out) {
+  const int nx = P->Nx, ny = P->Ny, nz = P->Nz;
+  for (int k = 0; k < nz; k++)
+    for (int j = 0; j < ny; j++)
+      for (int i = 0; i < nx; i++) {
+        const long s = i + (long)nx * (j + (long)ny * k);
+        out[s] = PT[s] != 0 ? lattice_order_parameter((float *)ni, PT, i, j, k, *P) : NAN;
+      }
 }
 
 extern "C" int ref_max_threads(void) { return (int)RNG.size(); }

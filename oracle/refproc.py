@@ -117,6 +117,12 @@ def _worker(m: dict, ops: List[tuple]) -> List[Any]:
             else:
                 used = L.ref_sweep(_p(ni), T, C.byref(a), None, 0, op[5] if len(op) > 5 else 0)
             out.append((ni, a.value, used))
+        elif kind == "local_order":
+            ni = np.ascontiguousarray(op[1], np.float32)
+            S = np.zeros(n, np.float32)
+            L.ref_local_order.argtypes = [C.c_void_p, C.c_void_p]
+            L.ref_local_order(_p(ni), _p(S))
+            out.append(S)
         elif kind == "energy":
             ni = np.ascontiguousarray(op[1], np.float32)
             out.append(float(L.ref_energy(_p(ni))))

@@ -1,4 +1,7 @@
 """Shared test helpers: descriptors from oracle models, the GPU fixture."""
+import json
+import os
+
 import numpy as np
 
 import mcx
@@ -99,3 +102,16 @@ def assert_stat_parity(checks, labels):
     allowed = chance_exceedances(n)
     assert len(bad) <= allowed and all(b[-1] <= 4.0 for b in bad), (n, allowed, bad)
     return bad
+
+
+def load_local_order():
+    """tests/golden/local_order.npz (make_local_order.py): per lattice its
+    model, point types, directors and the reference's local S."""
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "local_order.npz")
+    z = np.load(path)
+    out = {}
+    for name, d in json.loads(str(z["models"])).items():
+        d = dict(d)
+        d["surfaces"] = [O.Surface(**s) for s in d["surfaces"]]
+        out[name] = (O.Model(**d), z[f"{name}_pt"], z[f"{name}_ni"], z[f"{name}_S"])
+    return out

@@ -1,8 +1,9 @@
 """Snapshots, checkpoints, replica exchange and the parameter-file driver.
 
-- mcx_local_order against an FP64 NumPy restatement of
-  lattice_order_parameter (src/parameter_order.cpp:62-113): Q over the site and
-  its existing active neighbours, largest eigenvalue; NaN at inactive sites.
+- mcx_local_order against the reference's own lattice_order_parameter
+  (src/parameter_order.cpp:62-113) on committed golden states, and against
+  the oracle's FP64 restatement: Q over the site and its existing active
+  neighbours, largest eigenvalue; NaN at inactive sites.
 - mcx_save / mcx_load: a loaded engine continues the saved trajectory bit for
   bit (same states, step sizes and running sums after more sweeps).
 - mcx_exchange: the decisions are min(1, exp((1/Ta - 1/Tb)(Ha - Hb))) against
@@ -21,40 +22,22 @@ import pytest
 import mcx
 from oracle import oracle as O
 from oracle import replicas as OR
-from helpers import desc_from_model, random_state
+from helpers import desc_from_model, load_local_order, random_state
 
 pytestmark = pytest.mark.gpu
 
+LOCAL_ORDER = load_local_order()
 
-def local_S_ref(ni, pt, m):
-    nx, ny, nz = m.nx, m.ny, m.nz
-    xb, yb, zb = m.effective_bounds()
-    N = [nx, ny, nz]
-    B = [xb, yb, zb]
-    out = np.full(m.n, np.nan)
-    for s in np.nonzero(pt)[0]:
-        i, j, k = s % nx, (s // nx) % ny, s // (nx * ny)
-        Q = np.zeros((3, 3))
-        pts = 0
-        for d in ((0, 0, 0), (-1, 0, 0), (1, 0, 0), (0, -1, 0), (0, 1, 0), (0, 0, -1), (0, 0, 1)):
-            c = [i + d[0], j + d[1], k + d[2]]
-            ok = True
-            for ax in range(3):
-                if c[ax] < 0 or c[ax] >= N[ax]:
-                    if B[ax] == "periodic":
-                        c[ax] %= N[ax]
-                    else:
-                        ok = False
-            if not ok:
-                continue
-            t = c[0] + nx * (c[1] + ny * c[2])
-            if pt[t] == 0:
-                continue
-            n = ni[t].astype(np.float64)
-            Q += 3 * np.outer(n, n) - np.eye(3)
-            pts += 1
-        out[s] = np.linalg.eigvalsh(Q / (2 * pts))[-1]
-    return out
+
+@pytest.mark.parametrize("name", list(LOCAL_ORDER))
+def test_local_order_against_reference(name):
+    m, pt, ni, S = LOCAL_ORDER[name]
+    with mcx.Engine([desc_from_model(m)]) as eng:
+        eng.set_state(0, ni)
+        got = eng.local_order(0)
+    assert np.array_equal(np.isnan(got), np.isnan(S))
+    ok = ~np.isnan(S)
+    assert np.max(np.abs(got[ok] - S[ok])) < 1e-6
 
 
 @pytest.mark.parametrize("m", [O.Model(nx=12, ny=10, nz=8, potential="ll"),
@@ -72,7 +55,7 @@ def test_local_order_parameter(m):
         eng.set_state(0, ni)
         got = eng.local_order(0)
         ni = eng.get_state(0)
-    want = local_S_ref(ni, lat.pt, m)
+    want = O.local_order(ni, lat.pt, m)
     assert np.array_equal(np.isnan(got), np.isnan(want))
     ok = ~np.isnan(want)
     assert np.max(np.abs(got[ok] - want[ok])) < 2e-6
