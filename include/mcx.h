@@ -427,6 +427,13 @@ mcx_status mcx_polarization(mcx_engine *eng, int replica, double *P);
  * site, natural order.  Computed on the GPU. */
 mcx_status mcx_local_order(mcx_engine *eng, int replica, float *S);
 
+/* print_n (src/io.cpp:50-80): writes a replica's current state as the
+ * reference's snapshot file, header "x,y,z,nx,ny,nz,S,pt" and one
+ * "%d,%d,%d,%g,%g,%g,%g,%d" line per site in natural order, S the local
+ * order parameter (mcx_local_order; nan at inactive sites).  MCX_ERR_IO when
+ * the file cannot be written. */
+mcx_status mcx_print_n(mcx_engine *eng, int replica, const char *path);
+
 /* Checkpoint (no counterpart in the reference): every replica's descriptor,
  * directors, mask, temperature, step size, sweep and measured-sweep counters
  * (the Philox counters: a loaded engine continues the saved trajectory bit

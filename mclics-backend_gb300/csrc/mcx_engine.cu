@@ -183,6 +183,8 @@ extern "C" int mcx_version(void) { return 1; }
 
 extern "C" const char *mcx_last_error(const mcx_engine *e) { return e ? e->err.c_str() : g_last_error.c_str(); }
 
+void mcx::set_engine_error(mcx_engine *e, const char *msg) { e->err = msg ? msg : ""; }
+
 extern "C" int mcx_num_replicas(const mcx_engine *e) { return e ? e->nrep : 0; }
 
 extern "C" long long mcx_kernel_launches(const mcx_engine *e) { return e ? e->launches : 0; }

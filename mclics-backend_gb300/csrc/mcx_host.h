@@ -59,5 +59,7 @@ int parse_param_file(const char *path, SimParams &p, std::string &err);
 
 // Sets the message mcx_last_error(NULL) returns.
 void set_last_error(const char *msg);
+// the message mcx_last_error(e) returns
+void set_engine_error(mcx_engine *e, const char *msg);
 
 }  // namespace mcx

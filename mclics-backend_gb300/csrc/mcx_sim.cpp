@@ -468,3 +468,23 @@ extern "C" mcx_status mcx_check_file(const char *param_file, mcx_replica_desc *d
   if (desc) *desc = d;
   return MCX_OK;
 }
+
+extern "C" mcx_status mcx_print_n(mcx_engine *e, int r, const char *path) {
+  if (!e || !path) {
+    mcx::set_last_error("mcx_print_n: null engine or path");
+    return MCX_ERR_INVALID;
+  }
+  mcx_replica_desc d;
+  if (mcx_status st = mcx_get_desc(e, r, &d, nullptr)) return st;
+  const long n = (long)d.nx * d.ny * d.nz;
+  std::vector<float> ni(3 * n), ns(3 * n), S(n);
+  std::vector<int> pt(n);
+  if (mcx_status st = mcx_get_state(e, r, ni.data())) return st;
+  if (mcx_status st = mcx_get_mask(e, r, pt.data(), ns.data())) return st;
+  if (mcx_status st = mcx_local_order(e, r, S.data())) return st;
+  if (!mcx::write_snapshot(path, ni, pt, d, S.data())) {
+    mcx::set_engine_error(e, (std::string("mcx_print_n: cannot write ") + path).c_str());
+    return MCX_ERR_IO;
+  }
+  return MCX_OK;
+}

@@ -158,6 +158,7 @@ def lib() -> C.CDLL:
         L.mcx_sweep_timing.argtypes = [V, I, C.POINTER(F)]
         L.mcx_debug_barrier_timeout.argtypes = [V]
         L.mcx_local_order.argtypes = [V, I, V]
+        L.mcx_print_n.argtypes = [V, I, C.c_char_p]
         L.mcx_polarization.argtypes = [V, I, C.POINTER(C.c_double)]
         L.mcx_save.argtypes = [V, C.c_char_p]
         L.mcx_load.argtypes = [V, C.c_char_p]
@@ -386,6 +387,11 @@ class Engine:
         out = np.zeros(self.sites(r), np.float32)
         self._ck(self._L.mcx_local_order(self._h, r, _p(out)))
         return out
+
+    def print_n(self, r: int, path: str):
+        """The replica's current state as the reference's snapshot file
+        (print_n): x,y,z,nx,ny,nz,S,pt."""
+        self._ck(self._L.mcx_print_n(self._h, r, path.encode()))
 
     def save(self, path: str):
         self._ck(self._L.mcx_save(self._h, path.encode()))

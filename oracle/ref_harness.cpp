@@ -242,6 +242,12 @@ extern "C" void ref_local_order(const float *ni, float *out) {
       }
 }
 
+/* print_n (src/io.cpp:50-80): the reference's snapshot file of state ni. */
+extern "C" int ref_print_n(const float *ni, const char *path) {
+  memcpy(NI, ni, sizeof(float) * 3 * NT);
+  return print_n((char *)path, NI, *P, PT);
+}
+
 extern "C" int ref_max_threads(void) { return (int)RNG.size(); }
 
 /* The Pear potential (src/simulator.cpp:95-97) with its B1 and C, after ref_setup. */

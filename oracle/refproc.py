@@ -123,6 +123,13 @@ def _worker(m: dict, ops: List[tuple]) -> List[Any]:
             L.ref_local_order.argtypes = [C.c_void_p, C.c_void_p]
             L.ref_local_order(_p(ni), _p(S))
             out.append(S)
+        elif kind == "print_n":
+            ni = np.ascontiguousarray(op[1], np.float32)
+            L.ref_print_n.argtypes = [C.c_void_p, C.c_char_p]
+            if L.ref_print_n(_p(ni), op[2].encode()) != 0:
+                raise RuntimeError("print_n failed")
+            with open(op[2]) as f:
+                out.append(f.read())
         elif kind == "energy":
             ni = np.ascontiguousarray(op[1], np.float32)
             out.append(float(L.ref_energy(_p(ni))))

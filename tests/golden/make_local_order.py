@@ -1,7 +1,8 @@
-"""Writes local_order.npz: director states and the local order parameter
-that the reference's own lattice_order_parameter
-(src/parameter_order.cpp:62-113), compiled in oracle/_ref, returns for them
-at every active site (NaN elsewhere).  Four cases: periodic LL bulk, a
+"""Writes local_order.npz: director states, the local order parameter that
+the reference's own lattice_order_parameter (src/parameter_order.cpp:62-113),
+compiled in oracle/_ref, returns for them at every active site (NaN
+elsewhere), and, for the droplet and the slab, the snapshot file its print_n
+(src/io.cpp:50-80) writes for them.  Four cases: periodic LL bulk, a
 droplet with free bounds and a GHRL slab, each with seeded random directors
 tilted towards (0.1, 0.2, 0.9) (S about 0.86-0.99, an ordered snapshot), and
 the bulk with untilted random directors (low S, nearly degenerate Q).
@@ -15,6 +16,7 @@ import dataclasses
 import json
 import os
 import sys
+import tempfile
 
 import numpy as np
 
@@ -25,13 +27,15 @@ from oracle import oracle as O  # noqa: E402
 from oracle import refproc  # noqa: E402
 
 MODELS = {
-    "bulk": O.Model(nx=12, ny=10, nz=8, potential="ll"),
-    "sphere": O.Model(nx=14, ny=14, nz=14, geometry="sphere", xbound="free", ybound="free", zbound="free",
+    "bulk": O.Model(nx=10, ny=8, nz=6, potential="ll"),
+    "sphere": O.Model(nx=10, ny=10, nz=10, geometry="sphere", xbound="free", ybound="free", zbound="free",
                       potential="ll", surfaces=[O.Surface("fg", 1.0)]),
     "slab": O.Model(nx=12, ny=8, nz=6, geometry="slab", potential="ghrl",
                     surfaces=[O.Surface("homeotropic", 2.0), O.Surface("fg", 1.0)]),
-    "bulk_random": O.Model(nx=12, ny=10, nz=8, potential="ll"),
+    "bulk_random": O.Model(nx=10, ny=8, nz=6, potential="ll"),
 }
+
+CSV_CASES = ("sphere", "slab")  # snapshot text kept for these (inactive sites; surfaces)
 
 
 def state(m: O.Model, pt: np.ndarray, seed: int, tilt: bool) -> np.ndarray:
@@ -51,7 +55,10 @@ def main():
     for q, (name, m) in enumerate(MODELS.items()):
         ((pt, _),) = refproc.run(m, [("mask",)])
         ni = state(m, pt, 40 + q, tilt=name != "bulk_random")
-        (S,) = refproc.run(m, [("local_order", ni)])
+        with tempfile.TemporaryDirectory() as d:
+            S, csv = refproc.run(m, [("local_order", ni), ("print_n", ni, os.path.join(d, "snap.csv"))])
+        if name in CSV_CASES:
+            arrays[f"{name}_csv"] = np.frombuffer(csv.encode(), np.uint8)
         arrays[f"{name}_ni"] = ni
         arrays[f"{name}_pt"] = pt.astype(np.uint8)
         arrays[f"{name}_S"] = S

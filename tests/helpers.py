@@ -106,12 +106,14 @@ def assert_stat_parity(checks, labels):
 
 def load_local_order():
     """tests/golden/local_order.npz (make_local_order.py): per lattice its
-    model, point types, directors and the reference's local S."""
+    model, point types, directors, the reference's local S and the text of
+    the reference's snapshot file of that state (None where not kept)."""
     path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "local_order.npz")
     z = np.load(path)
     out = {}
     for name, d in json.loads(str(z["models"])).items():
         d = dict(d)
         d["surfaces"] = [O.Surface(**s) for s in d["surfaces"]]
-        out[name] = (O.Model(**d), z[f"{name}_pt"], z[f"{name}_ni"], z[f"{name}_S"])
+        csv = z[f"{name}_csv"].tobytes().decode() if f"{name}_csv" in z.files else None
+        out[name] = (O.Model(**d), z[f"{name}_pt"], z[f"{name}_ni"], z[f"{name}_S"], csv)
     return out

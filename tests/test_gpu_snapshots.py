@@ -31,13 +31,37 @@ LOCAL_ORDER = load_local_order()
 
 @pytest.mark.parametrize("name", list(LOCAL_ORDER))
 def test_local_order_against_reference(name):
-    m, pt, ni, S = LOCAL_ORDER[name]
+    m, pt, ni, S, _ = LOCAL_ORDER[name]
     with mcx.Engine([desc_from_model(m)]) as eng:
         eng.set_state(0, ni)
         got = eng.local_order(0)
     assert np.array_equal(np.isnan(got), np.isnan(S))
     ok = ~np.isnan(S)
     assert np.max(np.abs(got[ok] - S[ok])) < 1e-6
+
+
+@pytest.mark.parametrize("name", [k for k, v in LOCAL_ORDER.items() if v[4] is not None])
+def test_print_n_against_reference(name, tmp_path):
+    """mcx_print_n writes the reference's print_n file for the same state:
+    the same header, and per line the same coordinates, directors (the same
+    floats through %g), point type and nan text; S as the reference prints
+    it to within its FP32 evaluation (the two solve Q in different code, so
+    the sixth significant digit can differ)."""
+    m, pt, ni, S, csv = LOCAL_ORDER[name]
+    path = tmp_path / "snap.csv"
+    with mcx.Engine([desc_from_model(m)]) as eng:
+        eng.set_state(0, ni)
+        eng.print_n(0, str(path))
+    got, want = path.read_text().splitlines(), csv.splitlines()
+    assert got[0] == want[0] == "x,y,z,nx,ny,nz,S,pt"
+    assert len(got) == len(want) == m.n + 1
+    for a, b in zip(got[1:], want[1:]):
+        fa, fb = a.split(","), b.split(",")
+        assert fa[:6] == fb[:6] and fa[7] == fb[7], (a, b)
+        if fb[6] == "nan":
+            assert fa[6] == "nan", (a, b)
+        else:
+            assert abs(float(fa[6]) - float(fb[6])) <= 2e-6, (a, b)
 
 
 @pytest.mark.parametrize("m", [O.Model(nx=12, ny=10, nz=8, potential="ll"),

@@ -15,7 +15,7 @@ CASES = load_local_order()
 
 @pytest.mark.parametrize("name", list(CASES))
 def test_oracle_local_order_matches_reference_golden(name):
-    m, pt, ni, S = CASES[name]
+    m, pt, ni, S, _ = CASES[name]
     assert np.array_equal(O.Lattice(m).pt != 0, pt != 0)  # the oracle's mask is the reference's
     want = O.local_order(ni, pt, m)
     assert np.array_equal(np.isnan(S), np.isnan(want))
@@ -25,7 +25,8 @@ def test_oracle_local_order_matches_reference_golden(name):
 
 
 @pytest.mark.skipif(not refproc.available(), reason="reference build (oracle/_ref) not present")
-def test_local_order_golden_is_the_reference_output():
-    for name, (m, pt, ni, S) in CASES.items():
-        (got,) = refproc.run(m, [("local_order", ni)])
+def test_local_order_golden_is_the_reference_output(tmp_path):
+    for name, (m, pt, ni, S, csv) in CASES.items():
+        got, text = refproc.run(m, [("local_order", ni), ("print_n", ni, str(tmp_path / f"{name}.csv"))])
         assert np.array_equal(got, S, equal_nan=True), name
+        assert csv is None or text == csv, name
