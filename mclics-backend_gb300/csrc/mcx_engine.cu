@@ -79,6 +79,7 @@ struct mcx_engine {
   // per replica of a masked batch, row j + ny * k: 0 no active site, 1 only
   // bulk sites (point type 1), 2 anything else (empty: unknown)
   std::vector<std::vector<uint8_t>> rowact;
+  bool defer_plan = false;  // mcx_create / mcx_load: masks uploaded first, units planned once after
   // learned-proposal z-march: its own units (128 pairs x kLearnPlanes planes)
   std::vector<int4> lunits;
   int4 *d_lunits = nullptr;
@@ -300,6 +301,46 @@ static void mark_dead_units(mcx_engine *e) {
   }
 }
 
+// Plane runs of a replica for the z-march's chunks: maximal runs of planes k
+// whose units can all be bulk units (every row of planes k-1..k+1 that exist
+// holds bulk sites only) and runs of the other planes.  Chunks never straddle
+// two runs, so the planes at a slab's surfaces get short chunks of their own
+// and the rest of the replica runs the unmasked update.  One run for
+// unmasked replicas and for the persistent form (all units in one wave).
+static std::vector<int2> plane_runs(const mcx_engine *e, int r) {
+  const RepDev &R = e->rep[r];
+  const std::vector<uint8_t> &act = e->rowact[r];
+  std::vector<int2> runs;
+  if (act.empty() || e->pmarch) {
+    runs.push_back(make_int2(0, R.nz));
+    return runs;
+  }
+  std::vector<char> bulk(R.nz);
+  for (int k = 0; k < R.nz; k++) {
+    bool b = true;
+    for (int j = 0; j < R.ny && b; j++) b = act[(size_t)j + (size_t)R.ny * k] == 1;
+    bulk[k] = b;
+  }
+  auto eligible = [&](int k) {
+    for (int d = -1; d <= 1; d++) {
+      int kk = k + d;
+      if (kk < 0 || kk >= R.nz) {
+        if (R.zb != BOUND_PERIODIC) continue;
+        kk = (kk + R.nz) % R.nz;
+      }
+      if (!bulk[kk]) return false;
+    }
+    return true;
+  };
+  int k0 = 0;
+  for (int k = 1; k <= R.nz; k++)
+    if (k == R.nz || eligible(k) != eligible(k0)) {
+      runs.push_back(make_int2(k0, k));
+      k0 = k;
+    }
+  return runs;
+}
+
 static void plan_march(mcx_engine *e) {
   e->units.clear();
   const int nt = e->march_nt, np = unit_pairs(e);
@@ -331,21 +372,24 @@ static void plan_march(mcx_engine *e) {
     RepDev &R = e->rep[r];
     const int npp = R.hp * R.ny;
     R.mcta = 0;
-    if (march_k > 0) {
-      const int K = std::min(march_k, R.nz);
-      for (int k0 = 0; k0 < R.nz; k0 += K)
-        for (int p0 = 0; p0 < npp; p0 += np) {
-          e->units.push_back(make_int4(r, p0, k0, std::min(K, R.nz - k0)));
-          R.mcta++;
-        }
-    } else {
-      // rounded down, so that the units never exceed the waves asked for
-      const int chunks = std::max(1, std::min(R.nz, (int)std::floor(R.nz / avg)));
-      for (int q = 0; q < chunks; q++) {
-        const int k0 = (int)((long long)q * R.nz / chunks), k1 = (int)((long long)(q + 1) * R.nz / chunks);
-        for (int p0 = 0; p0 < npp; p0 += np) {
-          e->units.push_back(make_int4(r, p0, k0, k1 - k0));
-          R.mcta++;
+    for (const int2 run : plane_runs(e, r)) {
+      const int len = run.y - run.x;
+      if (march_k > 0) {
+        const int K = std::min(march_k, len);
+        for (int k0 = run.x; k0 < run.y; k0 += K)
+          for (int p0 = 0; p0 < npp; p0 += np) {
+            e->units.push_back(make_int4(r, p0, k0, std::min(K, run.y - k0)));
+            R.mcta++;
+          }
+      } else {
+        // rounded down, so that the units never exceed the waves asked for
+        const int chunks = std::max(1, std::min(len, (int)std::floor(len / avg)));
+        for (int q = 0; q < chunks; q++) {
+          const int k0 = run.x + (int)((long long)q * len / chunks), k1 = run.x + (int)((long long)(q + 1) * len / chunks);
+          for (int p0 = 0; p0 < npp; p0 += np) {
+            e->units.push_back(make_int4(r, p0, k0, k1 - k0));
+            R.mcta++;
+          }
         }
       }
     }
@@ -567,6 +611,7 @@ extern "C" mcx_status mcx_create(int n, const mcx_replica_desc *descs, mcx_engin
   }
   CKC(cudaMemcpyAsync(e->d_st, hs.data(), sizeof(RepState) * n, cudaMemcpyHostToDevice, e->stream));
   CKC(cudaStreamSynchronize(e->stream));
+  e->defer_plan = true;
   for (int r = 0; r < n; r++) {
     if (e->var.mask) {
       build_mask(e->desc[r], pt, ns);
@@ -578,6 +623,15 @@ extern "C" mcx_status mcx_create(int n, const mcx_replica_desc *descs, mcx_engin
       }
     }
     st = mcx_init_homogeneous(e, r, 0.f, 0.f);
+    if (st) {
+      g_last_error = e->err;
+      free_engine(e);
+      return st;
+    }
+  }
+  e->defer_plan = false;
+  if (e->var.mask) {
+    st = apply_march_shape(e, e->march_nt, e->march_k);
     if (st) {
       g_last_error = e->err;
       free_engine(e);
@@ -689,10 +743,13 @@ extern "C" mcx_status mcx_set_mask(mcx_engine *e, int r, const int *pt, const fl
     // an odd-nx row also holds a padding slot (inactive): never a bulk row
     act[row] = bulk && R.nx % 2 == 0 ? 1 : (any ? 2 : 0);
   }
-  mark_dead_units(e);
-  if (e->d_units && !e->units.empty())
-    CK(e, cudaMemcpyAsync(e->d_units, e->units.data(), sizeof(int4) * e->units.size(), cudaMemcpyHostToDevice,
-                          e->stream));
+  // the z-march's chunks follow the mask's plane runs: plan them again (in
+  // mcx_create and mcx_load once, after every replica's mask)
+  if (e->defer_plan) {
+    mark_dead_units(e);
+  } else if (mcx_status st = apply_march_shape(e, e->march_nt, e->march_k)) {
+    return st;
+  }
   if (e->d_lunits && !e->lunits.empty())
     CK(e, cudaMemcpyAsync(e->d_lunits, e->lunits.data(), sizeof(int4) * e->lunits.size(), cudaMemcpyHostToDevice,
                           e->stream));
@@ -1594,9 +1651,16 @@ extern "C" mcx_status mcx_load(mcx_engine *e, const char *path) {
   CK(e, cudaStreamSynchronize(e->stream));
   std::vector<RepState> st(n);
   CK(e, cudaMemcpy(st.data(), e->d_st, sizeof(RepState) * n, cudaMemcpyDeviceToHost));
+  e->defer_plan = true;
+  for (int r = 0; r < n && e->var.mask; r++)
+    if (mcx_status s2 = mcx_set_mask(e, r, pt[r].data(), ns[r].data())) {
+      e->defer_plan = false;
+      return s2;
+    }
+  e->defer_plan = false;
+  if (e->var.mask)
+    if (mcx_status s2 = apply_march_shape(e, e->march_nt, e->march_k)) return s2;
   for (int r = 0; r < n; r++) {
-    if (e->var.mask)
-      if (mcx_status s2 = mcx_set_mask(e, r, pt[r].data(), ns[r].data())) return s2;
     if (mcx_status s2 = mcx_set_state(e, r, ni[r].data())) return s2;
     st[r].T = cs[r].T;
     st[r].ang_var = cs[r].ang_var;
