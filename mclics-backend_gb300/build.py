@@ -17,7 +17,7 @@ EXTRA = os.environ.get("MCX_NVCC_FLAGS", "").split()
 NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 HOSTFLAGS = ["-fPIC", "-ffp-contract=off", "-O3", "-fno-strict-aliasing"]
-CUDA_TU = ["mcx_kernels.cu", "mcx_march.cu", "mcx_amarch.cu", "mcx_qmarch.cu", "mcx_pmarch.cu", "mcx_lmarch.cu", "mcx_learned.cu", "mcx_train.cu", "mcx_engine.cu", "mcx_noalloc.cu", "mcx_tcmlp.cu"]
+CUDA_TU = ["mcx_kernels.cu", "mcx_march.cu", "mcx_march_odd.cu", "mcx_amarch.cu", "mcx_qmarch.cu", "mcx_pmarch.cu", "mcx_lmarch.cu", "mcx_learned.cu", "mcx_train.cu", "mcx_engine.cu", "mcx_noalloc.cu", "mcx_tcmlp.cu"]
 HOST_TU = ["mcx_host.cpp", "mcx_sim.cpp"]
 LIB = os.path.join(OUT, "libmcx.so")
 CLI = os.path.join(OUT, "mc_sim_gb300")

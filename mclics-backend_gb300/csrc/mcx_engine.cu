@@ -482,6 +482,7 @@ extern "C" mcx_status mcx_create(int n, const mcx_replica_desc *descs, mcx_engin
     }
     // an odd nx needs the mask: its padding slots are inactive sites
     if (d.geometry != MCX_GEO_BULK || d.nx % 2) e->var.mask = true;
+    if (d.nx % 2) e->var.odd = true;
     if (d.xbound != MCX_BOUND_PERIODIC || d.ybound != MCX_BOUND_PERIODIC || d.zbound != MCX_BOUND_PERIODIC ||
         d.nx % 4 != 0)
       e->var.per = false;

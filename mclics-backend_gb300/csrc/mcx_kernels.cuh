@@ -17,6 +17,7 @@ struct Variant {
   bool mask;
   bool field;
   bool per;  // every replica periodic in x, y and z with nx a multiple of 4 (no mask)
+  bool odd = false;  // some replica has an odd nx (then the batch has a mask)
 };
 
 // What a pass launch does.
@@ -91,6 +92,8 @@ int pass_blocks_per_sm(const Variant &v, int mode);
 // dependent launch; the kernel waits for it before touching shared state).
 void launch_march(const Variant &v, int mode, const PassArgs &a, int nt, bool pdl, cudaStream_t st);
 bool march_block_ok(int nt);
+// the z-march kernel of a masked batch with an odd nx (mcx_march_odd.cu)
+const void *march_kernel_odd(const Variant &v, int mode, int nt);
 // The z-march with its rows staged in shared memory by bulk copies (unmasked
 // lattices): prepare (shared-memory attribute, residency) once per shape.
 bool tmarch_prepare(const Variant &v, int nt, int smem_bytes);

@@ -17,119 +17,17 @@
 //            chunk; the Philox key schedule once per thread.
 //
 // It computes what the other passes compute (same site_update, same Philox
-// counter: pair index row * hp + q, sweep, colour).  Results agree bit for
-// bit except where a decision lies within an ulp of its threshold: each
-// kernel inlines the update into different code and the compiler fuses its
-// multiply-adds (a*b + c*d as fma(a, b, c*d) or fma(c, d, a*b)) per kernel,
-// so about one decision in 10^7-10^8 updates can go the other way, after
-// which the trajectories part but sample the same states.  Each form is
-// deterministic run to run.
+// counter: pair index row * hp + q, sweep, colour), and as the energy change
+// fixes every rounding (bond_sum in mcx_pass.cuh), it runs the same chain bit
+// for bit.  The kernel template is in mcx_march_kernel.cuh; the variant for
+// masked batches with an odd nx is built in mcx_march_odd.cu.
 #include <cuda_runtime.h>
 
 #include "mcx_march.cuh"
+#include "mcx_march_kernel.cuh"
 #include "mcx_tma.cuh"
 
 namespace mcx {
-
-// One plane of the march: loads (first, so that the Philox rounds overlap
-// them), the pair update, the stores.
-template <int POT, bool MASK, bool FIELD, int MODE, bool PER>
-__device__ __forceinline__ void march_plane(const PassArgs &a, const RepDev &R, int c, const March &m,
-                                            const OPair &om, const OPair &o0, const OPair &op, bool zp, bool zm,
-                                            uint32_t seed, uint32_t stream, unsigned long long sw, float ang,
-                                            float invT, unsigned &acc, float qs[kQ]) {
-  float2 ax = *reinterpret_cast<const float2 *>(m.A0 + m.off);
-  float2 ay = *reinterpret_cast<const float2 *>(m.A1 + m.off);
-  float2 az = *reinterpret_cast<const float2 *>(m.A2 + m.off);
-  const int dx = m.s ? m.dx1 : m.dx0;
-  const float exv[3] = {ldo1(m.O0 + m.off + dx), ldo1(m.O1 + m.off + dx), ldo1(m.O2 + m.off + dx)};
-  OPair yp, ym;
-  load_opair_at<MASK>(m, m.off + m.dyp, m.offp + m.dypp, true, yp);
-  load_opair_at<MASK>(m, m.off + m.dym, m.offp + m.dymp, true, ym);
-  uint16_t pself = 0x0101;
-  uint8_t pex = 1;
-  if (MASK) {
-    pself = __ldg(reinterpret_cast<const uint16_t *>(m.PA + m.offp));
-    pex = __ldg(m.PO + m.offp + dx);
-    // two inactive sites: nothing moves, and an unmeasured sweep adds nothing
-    // (a warp of such pairs skips the draw and the arithmetic)
-    if (MODE == MODE_SWEEP && pself == 0) return;
-  }
-  update_pair<POT, MASK, FIELD, MODE, PER>(a, R, c, m.s, m.hasB, m.ee0, m.ee1, m.eyp, m.eym, o0, yp, ym, op, om, exv,
-                                           pself, pex, zp, zm, m.pid, m.off, seed, stream, sw, ang, invT, ax, ay, az,
-                                           acc, qs, m.tail);
-  *reinterpret_cast<float2 *>(m.A0 + m.off) = ax;
-  *reinterpret_cast<float2 *>(m.A1 + m.off) = ay;
-  *reinterpret_cast<float2 *>(m.A2 + m.off) = az;
-}
-
-// The march of one unit's chunk of planes kb..ke-1 (everything after the
-// dependency wait).
-template <int POT, bool MASK, bool FIELD, int MODE, bool PER>
-__device__ __forceinline__ void march_chunk(const PassArgs &a, const RepDev &R, int c, March &m, int kb, int ke,
-                                            const RepState *S, unsigned &acc, float qs[kQ]) {
-  const int nz = R.nz;
-  const bool zper = R.zb == BOUND_PERIODIC;
-  const uint32_t seed = R.seed, stream = R.stream;
-  const unsigned long long sw = S->sweep;
-  const float ang = S->ang_var, invT = 1.0f / S->T;
-  // the z pipeline: opposite pairs of this column at planes k-1, k, k+1
-  OPair om, o0, op;
-  const bool zm0 = kb > 0 || zper;
-  {
-    const int wrap = kb == 0 ? nz : 0;  // plane -1 is plane nz-1 when z is periodic
-    load_opair_at<MASK>(m, m.off + (wrap - 1) * m.dz, m.offp + (wrap - 1) * m.dzp, zm0, om);
-    load_opair_at<MASK>(m, m.off, m.offp, true, o0);
-  }
-  bool zm = zm0;
-#pragma unroll 1
-  for (int k = kb; k < ke; k++) {
-    const bool zp = k + 1 < nz || zper;
-    const int up = k + 1 < nz ? 1 : 1 - nz;
-    load_opair_at<MASK>(m, m.off + up * m.dz, m.offp + up * m.dzp, zp, op);
-    march_plane<POT, MASK, FIELD, MODE, PER>(a, R, c, m, om, o0, op, zp, zm, seed, stream, sw, ang, invT, acc, qs);
-    om = o0;
-    o0 = op;
-    zm = true;
-    m.off += m.dz;
-    m.offp += m.dzp;
-    m.pid += m.dpid;
-    m.row += R.ny;
-    m.s ^= 1;
-  }
-}
-
-template <int POT, bool MASK, bool FIELD, int MODE, int NT, bool PER>
-__global__ void __launch_bounds__(NT, march_min_blocks<POT, MASK, NT>()) k_march(PassArgs a) {
-  static_assert(MODE == MODE_SWEEP || MODE == MODE_SWEEP_MEASURE, "sweep modes only");
-  const int4 u = a.units[blockIdx.x];
-  const int r = u.x, c = a.colour;
-  const RepDev &R = a.reps[r];
-  const RepState *S = a.st + r;
-  unsigned acc = 0;
-  float qs[kQ];
-#pragma unroll
-  for (int q = 0; q < kQ; q++) qs[q] = 0.f;
-  const int p = u.y + (int)threadIdx.x;
-  if (p < R.hp * R.ny) {
-    March m;
-    march_init<MASK>(a, R, c, p, u.z, m);
-    const int kb = u.z, ke = u.z + (u.w & kUnitPlanes);
-    // everything above depends only on constants; the state and the
-    // directors may still be written by the previous pass (programmatic
-    // dependent launch lets this grid start while that one drains)
-    grid_dependency_wait(m);
-    if (MASK && (u.w & kUnitDead))
-      dead_unit<FIELD, MODE>(R, m, kb, ke, qs);
-    else if (MASK && (u.w & kUnitBulk))  // only bulk sites around: the unmasked update
-      march_chunk<POT, false, FIELD, MODE, false>(a, R, c, m, kb, ke, S, acc, qs);
-    else
-      march_chunk<POT, MASK, FIELD, MODE, PER>(a, R, c, m, kb, ke, S, acc, qs);
-  }
-  grid_dependency_wait();    // threads without a pair reach here without having waited
-  grid_launch_dependents();  // the next pass may start its set-up now
-  flush_replica<NT, MODE>(a, r, 1, (unsigned)R.mcta, acc, qs, MASK);
-}
 
 // ---------------------------------------------------------------------------
 // The z-march with its rows staged in shared memory by bulk copies (TMA).
@@ -337,8 +235,8 @@ __global__ void __launch_bounds__(NT, march_min_blocks<POT, false, NT>()) k_tmar
 // ---------------------------------------------------------------------------
 template <int POT, bool MASK, bool FIELD, int NT, bool PER>
 static const void *march_fn(int mode) {
-  return mode == MODE_SWEEP_MEASURE ? (const void *)k_march<POT, MASK, FIELD, MODE_SWEEP_MEASURE, NT, PER>
-                                    : (const void *)k_march<POT, MASK, FIELD, MODE_SWEEP, NT, PER>;
+  return mode == MODE_SWEEP_MEASURE ? (const void *)k_march<POT, MASK, FIELD, MODE_SWEEP_MEASURE, NT, PER, false>
+                                    : (const void *)k_march<POT, MASK, FIELD, MODE_SWEEP, NT, PER, false>;
 }
 
 template <int POT, bool FIELD, int NT>
@@ -364,6 +262,7 @@ static const void *march_fn_v(const Variant &v, int mode) {
 }
 
 static const void *march_kernel(const Variant &v, int mode, int nt) {
+  if (v.mask && v.odd) return march_kernel_odd(v, mode, nt);
   switch (nt) {
     case 64: return march_fn_v<64>(v, mode);
     case 256: return march_fn_v<256>(v, mode);

@@ -101,14 +101,15 @@ __device__ __forceinline__ void load_opair_at(const March &m, int off, int offp,
 
 // The thread's march state for pair p of the plane (p < hp * ny) of colour
 // c, starting at plane kb: its geometry, y rows, x extras and the offsets of
-// plane kb.  Constants only (no director or state reads).
-template <bool MASK>
+// plane kb.  Constants only (no director or state reads).  ODD false: the
+// batch has no odd nx, so no pair has a phantom slot (odd_tail).
+template <bool MASK, bool ODD = true>
 __device__ __forceinline__ void march_init(const PassArgs &a, const RepDev &R, int c, int p, int kb, March &m) {
     const int hs = R.hs, hps = R.hps, ny = R.ny, hx = R.hx;
     const int j = (int)fastdiv((uint32_t)p, R.hp_m, R.hp_p);
     const int h0 = 2 * (p - j * R.hp);
     m.hasB = h0 + 1 < hx;
-    m.tail = odd_tail<MASK>(R, h0);
+    m.tail = odd_tail<MASK, ODD>(R, h0);
     // the x neighbour outside the opposite pair: x- of A when s = 0, x+ of B
     // (or of A when the pair has no B) when s = 1
     int ex0 = h0 - 1, ex1 = m.hasB ? h0 + 2 : h0 + 1;

@@ -351,10 +351,11 @@ struct PairStage {
 // other colour's phantom, so it has no x+ bond -- and a phantom (i = nx) when
 // s = 1.  Phantoms have point type 0, never move and add nothing to a
 // measurement.  Returns 1 / 2 when site A / B of the pair at h0 is in that
-// slot, else 0 (always 0 in unmasked kernels: an odd-nx replica has a mask).
-template <bool MASK>
+// slot, else 0 (always 0 in unmasked kernels: an odd-nx replica has a mask;
+// and in kernels built with ODD false, for batches without an odd nx).
+template <bool MASK, bool ODD = true>
 __device__ __forceinline__ uint8_t odd_tail(const RepDev &R, int h0) {
-  if (!MASK || !(R.nx & 1)) return 0;
+  if (!MASK || !ODD || !(R.nx & 1)) return 0;
   return h0 == R.hx - 1 ? 1 : (h0 + 1 == R.hx - 1 ? 2 : 0);
 }
 
