@@ -45,8 +45,9 @@ constexpr uint32_t kLmarchTcCols = 128;  // two tiles of 64 FP32 accumulator col
 #endif
 
 // the tensor-core form holds 63 KB of shared memory: three CTAs per SM, so
-// each thread may use up to 170 registers
-template <int POT, bool MASK, bool FIELD, int MODE, bool TC>
+// each thread may use up to 170 registers.  ODD: the batch holds an odd nx
+// (phantom slots, odd_tail); built only for masked batches that need it.
+template <int POT, bool MASK, bool FIELD, int MODE, bool TC, bool ODD>
 __global__ void __launch_bounds__(kLPB, TC ? 3 : MCX_LMARCH_MIN_BLOCKS) k_lmarch(PassArgs a) {
   static_assert(MODE == MODE_SWEEP || MODE == MODE_SWEEP_MEASURE, "sweep modes only");
   extern __shared__ __align__(1024) uint8_t dyn[];
@@ -82,7 +83,7 @@ __global__ void __launch_bounds__(kLPB, TC ? 3 : MCX_LMARCH_MIN_BLOCKS) k_lmarch
   const bool valid = u.y + (int)threadIdx.x < npp;
   const int p = valid ? u.y + (int)threadIdx.x : npp - 1;  // lanes past the plane shadow the last pair
   March m;
-  march_init<MASK>(a, R, c, p, u.z, m);
+  march_init<MASK, ODD>(a, R, c, p, u.z, m);
   const int nz = R.nz, nx = R.nx;
   const bool zper = R.zb == BOUND_PERIODIC;
   const int kb = u.z, ke = u.z + (u.w & kUnitPlanes);
@@ -244,19 +245,25 @@ __global__ void __launch_bounds__(kLPB, TC ? 3 : MCX_LMARCH_MIN_BLOCKS) k_lmarch
   }
 }
 
-template <int POT, bool MASK, bool FIELD, bool TC>
+template <int POT, bool MASK, bool FIELD, bool TC, bool ODD = false>
 static const void *lmarch_fn(int mode) {
-  return mode == MODE_SWEEP_MEASURE ? (const void *)k_lmarch<POT, MASK, FIELD, MODE_SWEEP_MEASURE, TC>
-                                    : (const void *)k_lmarch<POT, MASK, FIELD, MODE_SWEEP, TC>;
+  return mode == MODE_SWEEP_MEASURE ? (const void *)k_lmarch<POT, MASK, FIELD, MODE_SWEEP_MEASURE, TC, ODD>
+                                    : (const void *)k_lmarch<POT, MASK, FIELD, MODE_SWEEP, TC, ODD>;
+}
+
+template <int POT, bool FIELD, bool TC>
+static const void *lmarch_fn_masked(const Variant &v, int mode) {
+  return v.odd ? lmarch_fn<POT, true, FIELD, TC, true>(mode) : lmarch_fn<POT, true, FIELD, TC, false>(mode);
 }
 
 template <bool TC>
 static const void *lmarch_kernel_tc(const Variant &v, int mode) {
   if (v.pot == POT_LL) {
-    if (v.mask) return v.field ? lmarch_fn<POT_LL, true, true, TC>(mode) : lmarch_fn<POT_LL, true, false, TC>(mode);
+    if (v.mask) return v.field ? lmarch_fn_masked<POT_LL, true, TC>(v, mode) : lmarch_fn_masked<POT_LL, false, TC>(v, mode);
     return v.field ? lmarch_fn<POT_LL, false, true, TC>(mode) : lmarch_fn<POT_LL, false, false, TC>(mode);
   }
-  if (v.mask) return v.field ? lmarch_fn<POT_GHRL, true, true, TC>(mode) : lmarch_fn<POT_GHRL, true, false, TC>(mode);
+  if (v.mask)
+    return v.field ? lmarch_fn_masked<POT_GHRL, true, TC>(v, mode) : lmarch_fn_masked<POT_GHRL, false, TC>(v, mode);
   return v.field ? lmarch_fn<POT_GHRL, false, true, TC>(mode) : lmarch_fn<POT_GHRL, false, false, TC>(mode);
 }
 

@@ -126,7 +126,12 @@ IDENTITY_CASES = {**CASES,
                   # a small droplet in a large box: units with no active site around are skipped
                   "droplet_big_box": O.Model(nx=32, ny=32, nz=40, geometry="sphere", potential="ghrl", k11=1.0,
                                              k22=0.6, k33=1.4, p0=20, elecA=0.3, elecZ=1.0, elecE=1.5, radius=6.0,
-                                             surfaces=[O.Surface("fg", 1.0)])}
+                                             surfaces=[O.Surface("fg", 1.0)]),
+                  # odd lengths: the learned passes built with phantom-slot handling
+                  "droplet_odd13": O.Model(nx=13, ny=13, nz=13, geometry="sphere", potential="ghrl", k11=1.0,
+                                           k22=0.6, k33=1.4, p0=20, elecA=0.3, elecZ=1.0, elecE=1.5,
+                                           surfaces=[O.Surface("fg", 1.0)]),
+                  "bulk_ll_odd_free": O.Model(nx=9, ny=8, nz=6, xbound="free", potential="ll")}
 
 
 @pytest.mark.parametrize("name", list(IDENTITY_CASES))
