@@ -79,6 +79,11 @@ struct mcx_engine {
   // per replica of a masked batch, row j + ny * k: 0 no active site, 1 only
   // bulk sites (point type 1), 2 anything else (empty: unknown)
   std::vector<std::vector<uint8_t>> rowact;
+  // per replica of a masked batch cut into tiles (tiled[r]): the class (as
+  // rowact) of row j + ny * k over the x range of tile column s, with the x
+  // neighbours on either side: segact[r][(j + ny * k) * nseg + s]
+  std::vector<std::vector<uint8_t>> segact;
+  std::vector<char> tiled;
   bool defer_plan = false;  // mcx_create / mcx_load: masks uploaded first, units planned once after
   // learned-proposal z-march: its own units (128 pairs x kLearnPlanes planes)
   std::vector<int4> lunits;
@@ -264,6 +269,29 @@ static int unit_class(const mcx_engine *e, const int4 &u, int nt) {
   const std::vector<uint8_t> &act = e->rowact[u.x];
   if (act.empty()) return 0;
   const RepDev &R = e->rep[u.x];
+  if (u.w & kUnitTiled) {  // the tile's rows, over its x range (segact), and the rows and planes next to them
+    const std::vector<uint8_t> &seg = e->segact[u.x];
+    const int nseg = (R.hp + kTileW - 1) / kTileW;
+    const int j0 = u.y >> kTileQBits, sc = (u.y & ((1 << kTileQBits) - 1)) / kTileW;
+    const int j1 = std::min(j0 + nt / kTileW, R.ny) - 1, nk = u.w & kUnitPlanes;
+    unsigned seen = 0;
+    for (int k = u.z - 1; k <= u.z + nk; k++) {
+      int kk = k;
+      if (kk < 0 || kk >= R.nz) {
+        if (R.zb != BOUND_PERIODIC) continue;
+        kk = (kk + R.nz) % R.nz;
+      }
+      for (int j = j0 - 1; j <= j1 + 1; j++) {
+        int jj = j;
+        if (jj < 0 || jj >= R.ny) {
+          if (R.yb != BOUND_PERIODIC) continue;
+          jj = (jj + R.ny) % R.ny;
+        }
+        seen |= 1u << seg[((size_t)jj + (size_t)R.ny * kk) * nseg + sc];
+      }
+    }
+    return seen == 1u ? kUnitDead : (seen == 2u ? kUnitBulk : 0);
+  }
   const int pend = std::min(u.y + nt, R.hp * R.ny);
   const int j0 = u.y / R.hp, j1 = (pend - 1) / R.hp, nk = u.w & kUnitPlanes;
   unsigned seen = 0;  // bit c: a row of class c
@@ -294,7 +322,7 @@ static bool unit_dead(const mcx_engine *e, const int4 &u) { return unit_class(e,
 // Flags of the z-march units and of the learned z-march's units (which only
 // use kUnitDead).
 static void mark_dead_units(mcx_engine *e) {
-  for (int4 &u : e->units) u.w = (u.w & kUnitPlanes) | unit_class(e, u, unit_pairs(e));
+  for (int4 &u : e->units) u.w = (u.w & (kUnitPlanes | kUnitTiled)) | unit_class(e, u, unit_pairs(e));
   for (int4 &u : e->lunits) {
     const int cls = unit_class(e, u, lmarch_block_threads());
     u.w = (u.w & kUnitPlanes) | (cls == kUnitDead ? kUnitDead : 0);
@@ -341,6 +369,17 @@ static std::vector<int2> plane_runs(const mcx_engine *e, int r) {
   return runs;
 }
 
+// Whether the z-march cuts replica r into tiles (kUnitTiled): a masked
+// replica, some of whose rows cross the mask's edge, with rows at least two
+// tiles wide; not for the persistent form (whose units must fit one wave) nor
+// the four-site form (unmasked), nor an odd nx (phantom slots sit at the row
+// ends).
+static bool use_tiles(const mcx_engine *e, int r) {
+  const RepDev &R = e->rep[r];
+  return e->var.mask && !e->var.odd && !e->pmarch && !e->qmarch && r < (int)e->tiled.size() && e->tiled[r] &&
+         R.hp >= 2 * kTileW && R.hp < (1 << kTileQBits);
+}
+
 static void plan_march(mcx_engine *e) {
   e->units.clear();
   const int nt = e->march_nt, np = unit_pairs(e);
@@ -362,6 +401,13 @@ static void plan_march(mcx_engine *e) {
     for (int r = 0; r < e->nrep; r++) {
       const RepDev &R = e->rep[r];
       const int npp = R.hp * R.ny;
+      if (use_tiles(e, r)) {
+        for (int j0 = 0; j0 < R.ny; j0 += nt / kTileW)
+          for (int q0 = 0; q0 < R.hp; q0 += kTileW)
+            for (int k = 0; k < R.nz; k++)
+              work += !unit_dead(e, make_int4(r, (j0 << kTileQBits) | q0, k, 1 | kUnitTiled)) ? 1 : 0;
+        continue;
+      }
       for (int p0 = 0; p0 < npp; p0 += np)
         for (int k = 0; k < R.nz; k++)
           work += e->pmarch || !unit_dead(e, make_int4(r, p0, k, 1)) ? 1 : 0;
@@ -372,24 +418,34 @@ static void plan_march(mcx_engine *e) {
     RepDev &R = e->rep[r];
     const int npp = R.hp * R.ny;
     R.mcta = 0;
+    const bool tiles = use_tiles(e, r);
+    // the units of one chunk of planes k0 .. k0 + nk - 1: NT consecutive pairs
+    // of the plane, or tiles
+    auto chunk = [&](int k0, int nk) {
+      if (tiles) {
+        for (int j0 = 0; j0 < R.ny; j0 += nt / kTileW)
+          for (int q0 = 0; q0 < R.hp; q0 += kTileW) {
+            e->units.push_back(make_int4(r, (j0 << kTileQBits) | q0, k0, nk | kUnitTiled));
+            R.mcta++;
+          }
+        return;
+      }
+      for (int p0 = 0; p0 < npp; p0 += np) {
+        e->units.push_back(make_int4(r, p0, k0, nk));
+        R.mcta++;
+      }
+    };
     for (const int2 run : plane_runs(e, r)) {
       const int len = run.y - run.x;
       if (march_k > 0) {
         const int K = std::min(march_k, len);
-        for (int k0 = run.x; k0 < run.y; k0 += K)
-          for (int p0 = 0; p0 < npp; p0 += np) {
-            e->units.push_back(make_int4(r, p0, k0, std::min(K, run.y - k0)));
-            R.mcta++;
-          }
+        for (int k0 = run.x; k0 < run.y; k0 += K) chunk(k0, std::min(K, run.y - k0));
       } else {
         // rounded down, so that the units never exceed the waves asked for
         const int chunks = std::max(1, std::min(len, (int)std::floor(len / avg)));
         for (int q = 0; q < chunks; q++) {
           const int k0 = run.x + (int)((long long)q * len / chunks), k1 = run.x + (int)((long long)(q + 1) * len / chunks);
-          for (int p0 = 0; p0 < npp; p0 += np) {
-            e->units.push_back(make_int4(r, p0, k0, k1 - k0));
-            R.mcta++;
-          }
+          chunk(k0, k1 - k0);
         }
       }
     }
@@ -424,6 +480,8 @@ extern "C" mcx_status mcx_create(int n, const mcx_replica_desc *descs, mcx_engin
   long long dir_total = 0, pt_total = 0;
   e->rep.resize(n);
   e->rowact.resize(n);
+  e->segact.resize(n);
+  e->tiled.assign(n, 0);
   for (int r = 0; r < n; r++) {
     mcx_replica_desc &d = e->desc[r];
     effective_bounds(d);
@@ -743,6 +801,38 @@ extern "C" mcx_status mcx_set_mask(mcx_engine *e, int r, const int *pt, const fl
     }
     // an odd-nx row also holds a padding slot (inactive): never a bulk row
     act[row] = bulk && R.nx % 2 == 0 ? 1 : (any ? 2 : 0);
+  }
+  // rows that cross the mask's edge (active and inactive sites): cut the
+  // replica into tiles, classed over each tile column's x range (with the x
+  // neighbours on either side)
+  {
+    bool mixed = false;
+    for (long row = 0; row < (long)R.ny * R.nz && !mixed; row++) {
+      bool any = false, none = false;
+      for (int i = 0; i < R.nx; i++) (pt[row * R.nx + i] != 0 ? any : none) = true;
+      mixed = any && none;
+    }
+    e->tiled[r] = mixed;
+    std::vector<uint8_t> &seg = e->segact[r];
+    seg.clear();
+    if (mixed) {
+      const int nseg = (R.hp + kTileW - 1) / kTileW, w = 4 * kTileW;  // x sites per tile column
+      seg.assign((size_t)R.ny * R.nz * nseg, 0);
+      for (long row = 0; row < (long)R.ny * R.nz; row++)
+        for (int sc = 0; sc < nseg; sc++) {
+          bool any = false, bulk = true;
+          for (int x = sc * w - 1; x <= (sc + 1) * w; x++) {
+            int xx = x;
+            if (xx < 0 || xx >= R.nx) {
+              if (R.xb != BOUND_PERIODIC) continue;
+              xx = (xx + R.nx) % R.nx;
+            }
+            any |= pt[row * R.nx + xx] != 0;
+            bulk &= pt[row * R.nx + xx] == 1;
+          }
+          seg[(size_t)row * nseg + sc] = bulk && R.nx % 2 == 0 ? 1 : (any ? 2 : 0);
+        }
+    }
   }
   // the z-march's chunks follow the mask's plane runs: plan them again (in
   // mcx_create and mcx_load once, after every replica's mask)

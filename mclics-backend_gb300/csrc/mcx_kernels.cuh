@@ -40,7 +40,16 @@ constexpr int kUnitDead = 1 << 30;
 // the unmasked update, which gives the same result there without the mask's
 // loads and weights.
 constexpr int kUnitBulk = 1 << 29;
-constexpr int kUnitPlanes = kUnitBulk - 1;
+// kUnitTiled marks a unit of the z-march that is a tile of kTileW pairs of a
+// row times NT / kTileW rows (its second field (j0 << 12) | q0: first row,
+// first pair of the row) rather than NT consecutive pairs of the plane.
+// Masked replicas whose rows cross the mask's edge (droplets) are cut into
+// tiles, so that the units inside the droplet hold only bulk sites and run
+// the unmasked update.
+constexpr int kUnitTiled = 1 << 28;
+constexpr int kUnitPlanes = kUnitTiled - 1;
+constexpr int kTileLg = 2, kTileW = 1 << kTileLg;  // pairs per tile row (one 32-byte sector)
+constexpr int kTileQBits = 12;                      // q0 field: hp < 4096
 
 struct PassArgs {
   const RepDev *reps;

@@ -89,8 +89,15 @@ __global__ void __launch_bounds__(NT, march_min_blocks<POT, MASK, NT>()) k_march
   float qs[kQ];
 #pragma unroll
   for (int q = 0; q < kQ; q++) qs[q] = 0.f;
-  const int p = u.y + (int)threadIdx.x;
-  if (p < R.hp * R.ny) {
+  int p = u.y + (int)threadIdx.x;
+  bool live = p < R.hp * R.ny;
+  if (MASK && (u.w & kUnitTiled)) {  // a tile: kTileW pairs of each of NT / kTileW rows
+    const int q = (u.y & ((1 << kTileQBits) - 1)) + ((int)threadIdx.x & (kTileW - 1));
+    const int j = (u.y >> kTileQBits) + ((int)threadIdx.x >> kTileLg);
+    live = q < R.hp && j < R.ny;
+    p = j * R.hp + q;
+  }
+  if (live) {
     March m;
     march_init<MASK, ODD>(a, R, c, p, u.z, m);
     const int kb = u.z, ke = u.z + (u.w & kUnitPlanes);

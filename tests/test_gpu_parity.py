@@ -442,13 +442,16 @@ def test_large_lattice_kernels_agree(dims):
 def test_bulk_and_dead_units_agree_with_direct_pass(pot):
     """Masked lattices whose z-march units include bulk units (only point
     type 1 around: the unmasked update) and dead units (no active site
-    around): a deep slab and a small droplet in a large box.  Bit-identical
-    to the direct pass."""
+    around): a deep slab, a small droplet in a large box, and a droplet wide
+    enough (rows of 20 pairs) to be cut into tiles (kUnitTiled), some inside
+    the droplet (bulk tiles).  Bit-identical to the direct pass."""
     slab = O.Model(nx=16, ny=16, nz=48, geometry="slab", potential=pot, k11=1.0, k22=0.8, k33=1.2, elecA=0.4,
                    elecZ=1.0, elecE=1.0, surfaces=[O.Surface("homeotropic", 4.0), O.Surface("homeotropic", 4.0)])
     drop = O.Model(nx=32, ny=32, nz=32, geometry="sphere", potential=pot, k11=1.0, k22=0.6, k33=1.4, p0=20,
                    elecA=0.3, elecZ=1.0, elecE=1.5, radius=6.0, surfaces=[O.Surface("fg", 1.0)])
-    for m in (slab, drop):
+    wide = O.Model(nx=80, ny=72, nz=72, geometry="sphere", potential=pot, k11=1.0, k22=0.6, k33=1.4, p0=20,
+                   elecA=0.3, elecZ=1.0, elecE=1.5, radius=34.0, surfaces=[O.Surface("fg", 1.0)])
+    for m in (slab, drop, wide):
         d = desc_from_model(m, T=0.9, seed=31, stream=5)
         pt = O.Lattice(m).pt
 
