@@ -10,6 +10,22 @@
 
 namespace mcx {
 
+// What a measured pass adds for an active site of an unmasked lattice other
+// than its bonds (site_update): its Q-tensor products and field energy.
+template <bool FIELD>
+__device__ __forceinline__ void measure_opposite(const RepDev &R, float x, float y, float z, float qs[kQ]) {
+  qs[2] += x * x;
+  qs[3] += x * y;
+  qs[4] += x * z;
+  qs[5] += y * y;
+  qs[6] += y * z;
+  if (FIELD) {
+    const float ef = field_energy(R, x, y, z);
+    qs[0] += ef;
+    qs[1] += ef;
+  }
+}
+
 // One plane of the march: loads (first, so that the Philox rounds overlap
 // them), the pair update, the stores.
 template <int POT, bool MASK, bool FIELD, int MODE, bool PER>
@@ -37,6 +53,12 @@ __device__ __forceinline__ void march_plane(const PassArgs &a, const RepDev &R, 
   update_pair<POT, MASK, FIELD, MODE, PER>(a, R, c, m.s, m.hasB, m.ee0, m.ee1, m.eyp, m.eym, o0, yp, ym, op, om, exv,
                                            pself, pex, zp, zm, m.pid, m.off, seed, stream, sw, ang, invT, ax, ay, az,
                                            acc, qs, m.tail);
+  if (!MASK && MODE == MODE_SWEEP_MEASURE && a.meas_both) {
+    // the colour-0 pair of this row (final: its pass is done), as the colour-0
+    // pass's site_update would measure it
+    measure_opposite<FIELD>(R, o0.v[0].x, o0.v[1].x, o0.v[2].x, qs);
+    if (m.hasB) measure_opposite<FIELD>(R, o0.v[0].y, o0.v[1].y, o0.v[2].y, qs);
+  }
   *reinterpret_cast<float2 *>(m.A0 + m.off) = ax;
   *reinterpret_cast<float2 *>(m.A1 + m.off) = ay;
   *reinterpret_cast<float2 *>(m.A2 + m.off) = az;
