@@ -932,10 +932,10 @@ static PassArgs pass_args(mcx_engine *e) {
 static void launch_sweep_pass(mcx_engine *e, PassArgs &pa, int colour, bool measure) {
   pa.colour = colour;
   int mode = measure ? MODE_SWEEP_MEASURE : MODE_SWEEP;
-  // the plain register z-march of an unmasked batch measures both colours in
-  // its colour-1 pass (PassArgs::meas_both)
-  const bool both = e->proposal == MCX_PROPOSAL_PLAIN && !e->staged && e->march && !e->tmarch && !e->amarch &&
-                    !e->qmarch && !e->var.mask;
+  // the plain z-march of an unmasked batch (register, prefetching and
+  // four-site forms) measures both colours in its colour-1 pass
+  // (PassArgs::meas_both)
+  const bool both = e->proposal == MCX_PROPOSAL_PLAIN && !e->staged && e->march && !e->tmarch && !e->var.mask;
   pa.meas_both = measure && both ? 1 : 0;
   if (measure && both && colour == 0) mode = MODE_SWEEP;
   if (e->proposal == MCX_PROPOSAL_VMF_MLP) {

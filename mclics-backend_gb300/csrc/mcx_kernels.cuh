@@ -80,7 +80,8 @@ struct PassArgs {
   int nunits;
   // TMA-staged z-march: floats per O slot and per A slot of shared memory
   int tm_o, tm_a;
-  // measured sweeps of an unmasked batch on the register z-march: the colour-0
+  // measured sweeps of an unmasked batch on the z-march (register, prefetching
+  // and four-site forms): the colour-0
   // pass runs unmeasured and the colour-1 pass (MODE_SWEEP_MEASURE) also adds
   // the Q-tensor and field terms of the colour-0 sites, read from the opposite
   // pairs it loads anyway (one reduction per sweep instead of two)

@@ -29,6 +29,22 @@ __device__ __forceinline__ float ldo1(const float *p) { return __ldcg(p); }
 __device__ __forceinline__ void grid_dependency_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 __device__ __forceinline__ void grid_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;" :::); }
 
+// What a measured pass adds for an active site of an unmasked lattice other
+// than its bonds (site_update): its Q-tensor products and field energy.
+template <bool FIELD>
+__device__ __forceinline__ void measure_opposite(const RepDev &R, float x, float y, float z, float qs[kQ]) {
+  qs[2] += x * x;
+  qs[3] += x * y;
+  qs[4] += x * z;
+  qs[5] += y * y;
+  qs[6] += y * z;
+  if (FIELD) {
+    const float ef = field_energy(R, x, y, z);
+    qs[0] += ef;
+    qs[1] += ef;
+  }
+}
+
 // Opposite-colour pair of one row: 3 components (and point types).
 struct OPair {
   float2 v[3];

@@ -10,22 +10,6 @@
 
 namespace mcx {
 
-// What a measured pass adds for an active site of an unmasked lattice other
-// than its bonds (site_update): its Q-tensor products and field energy.
-template <bool FIELD>
-__device__ __forceinline__ void measure_opposite(const RepDev &R, float x, float y, float z, float qs[kQ]) {
-  qs[2] += x * x;
-  qs[3] += x * y;
-  qs[4] += x * z;
-  qs[5] += y * y;
-  qs[6] += y * z;
-  if (FIELD) {
-    const float ef = field_energy(R, x, y, z);
-    qs[0] += ef;
-    qs[1] += ef;
-  }
-}
-
 // One plane of the march: loads (first, so that the Philox rounds overlap
 // them), the pair update, the stores.
 template <int POT, bool MASK, bool FIELD, int MODE, bool PER>
