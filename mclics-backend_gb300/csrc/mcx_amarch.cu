@@ -111,7 +111,7 @@ __global__ void __launch_bounds__(NT, march_min_blocks<POT, false, NT>()) k_amar
       update_pair_draw<POT, false, FIELD, MODE, PER>(a, R, c, m.s, m.hasB, m.ee0, m.ee1, m.eyp, m.eym, o0, yp, ym, op,
                                                      om, exv, 0x0101, 1, zp, zm, rw, m.off, ang, invT, ax, ay, az, acc,
                                                      qs);
-      if (MODE == MODE_SWEEP_MEASURE && a.meas_both) {  // the colour-0 pair of this row (PassArgs::meas_both)
+      if (MODE == MODE_SWEEP_MEASURE && a.meas_both && c == 1) {  // the colour-0 pair of this row (PassArgs::meas_both)
         measure_opposite<FIELD>(R, o0.v[0].x, o0.v[1].x, o0.v[2].x, qs);
         if (m.hasB) measure_opposite<FIELD>(R, o0.v[0].y, o0.v[1].y, o0.v[2].y, qs);
       }

@@ -37,7 +37,7 @@ __device__ __forceinline__ void march_plane(const PassArgs &a, const RepDev &R, 
   update_pair<POT, MASK, FIELD, MODE, PER>(a, R, c, m.s, m.hasB, m.ee0, m.ee1, m.eyp, m.eym, o0, yp, ym, op, om, exv,
                                            pself, pex, zp, zm, m.pid, m.off, seed, stream, sw, ang, invT, ax, ay, az,
                                            acc, qs, m.tail);
-  if (!MASK && MODE == MODE_SWEEP_MEASURE && a.meas_both) {
+  if (!MASK && MODE == MODE_SWEEP_MEASURE && a.meas_both && c == 1) {
     // the colour-0 pair of this row (final: its pass is done), as the colour-0
     // pass's site_update would measure it
     measure_opposite<FIELD>(R, o0.v[0].x, o0.v[1].x, o0.v[2].x, qs);

@@ -163,7 +163,7 @@ __global__ void __launch_bounds__(NT, qmarch_min_blocks<NT>()) k_qmarch(PassArgs
       update_pair_draw<POT, false, FIELD, MODE, PER>(a, R, c, s, true, 1.f, ee1, eyp, eym, hi_pair(o0), hi_pair(yp),
                                                      hi_pair(ym), hi_pair(op), hi_pair(om), xB, 0x0101, 1, zp, zm,
                                                      rwB, off + 2, ang, invT, axB, ayB, azB, acc, qs);
-      if (MODE == MODE_SWEEP_MEASURE && a.meas_both) {  // the colour-0 quad of this row (PassArgs::meas_both)
+      if (MODE == MODE_SWEEP_MEASURE && a.meas_both && c == 1) {  // the colour-0 quad of this row (PassArgs::meas_both)
         measure_opposite<FIELD>(R, o0.v[0].x, o0.v[1].x, o0.v[2].x, qs);
         measure_opposite<FIELD>(R, o0.v[0].y, o0.v[1].y, o0.v[2].y, qs);
         measure_opposite<FIELD>(R, o0.v[0].z, o0.v[1].z, o0.v[2].z, qs);
