@@ -261,7 +261,7 @@ def other_workloads():
     for prop in ("vmf_mlp", "plain"):
         r = workloads.run_c5(replicas=64, sweeps=20, proposal=prop)
         c5[prop] = {k: r[k] for k in ("site_updates_per_s", "active_site_updates_per_s", "acceptance",
-                                      "pass_kernel", "seconds") if k in r}
+                                      "pass_kernel", "seconds", "sweep_ms", "roofline") if k in r}
         if "train_loss" in r:
             c5[prop]["train_loss_first_last"] = r["train_loss"]
     out["c5"] = {"workload": "64 droplets r=40 in 96^3, GHRL p0=20, planar W=1, field E=0..2.0 by 0.1 at T=0.8",

@@ -141,6 +141,21 @@ def run_c5(replicas=64, sweeps=20, proposal="plain", side=96, radius=40.0, train
         out["active_sites_per_replica"] = int(valid)
         out["acceptance"] = float(np.mean([x[ST_ACC] / (x[ST_SWEEPS] * valid) for x in st]))
         out["mean_S_last_field"] = float(np.mean([x[ST_S1] / max(x[ST_N], 1) for x in st]))
+        if proposal == "plain":
+            # the pass against the HBM roofline as for c3: 19 B per site of the
+            # box per pass (dead units load nothing, so this counts more than
+            # the pass moves), over the unmeasured sweep time
+            import ctypes as C
+            from . import lib
+            ms = C.c_float()
+            if lib().mcx_sweep_timing(eng._h, 80, C.byref(ms)) == 0:
+                sw_ms = ms.value / 80
+                peak, src = _peak()
+                ach = BYTES_PER_SITE_PASS_MASKED * sites / (sw_ms / 2 * 1e-3) / 1e9
+                out["sweep_ms"] = sw_ms
+                out["roofline"] = {"achieved_gbs": ach, "peak_gbs": peak, "frac": ach / peak, "peak_source": src,
+                                   "bytes_per_site_pass": BYTES_PER_SITE_PASS_MASKED,
+                                   "sites": "every site of the box"}
     out["site_updates_per_s"] = 2 * sweeps * len(fields) * sites / dt
     out["active_site_updates_per_s"] = 2 * sweeps * len(fields) * replicas * out["active_sites_per_replica"] / dt
     out["seconds"] = dt
