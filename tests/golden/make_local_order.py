@@ -1,7 +1,7 @@
 """Writes local_order.npz: director states, the local order parameter that
 the reference's own lattice_order_parameter (src/parameter_order.cpp:62-113),
 compiled in oracle/_ref, returns for them at every active site (NaN
-elsewhere), and, for the droplet and the slab, the snapshot file its print_n
+elsewhere), and, for the bulk, the droplet and the slab, the snapshot file its print_n
 (src/io.cpp:50-80) writes for them.  Four cases: periodic LL bulk, a
 droplet with free bounds and a GHRL slab, each with seeded random directors
 tilted towards (0.1, 0.2, 0.9) (S about 0.86-0.99, an ordered snapshot), and
@@ -35,7 +35,7 @@ MODELS = {
     "bulk_random": O.Model(nx=10, ny=8, nz=6, potential="ll"),
 }
 
-CSV_CASES = ("sphere", "slab")  # snapshot text kept for these (inactive sites; surfaces)
+CSV_CASES = ("bulk", "sphere", "slab")  # snapshot text kept for these (periodic; inactive sites; surfaces)
 
 
 def state(m: O.Model, pt: np.ndarray, seed: int, tilt: bool) -> np.ndarray:

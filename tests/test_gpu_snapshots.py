@@ -64,6 +64,15 @@ def test_print_n_against_reference(name, tmp_path):
             assert abs(float(fa[6]) - float(fb[6])) <= 2e-6, (a, b)
 
 
+def test_print_n_reports_an_unwritable_path(tmp_path):
+    m, pt, ni, S, _ = LOCAL_ORDER["bulk"]
+    with mcx.Engine([desc_from_model(m)]) as eng:
+        with pytest.raises(mcx.McxError) as err:
+            eng.print_n(0, str(tmp_path / "missing_dir" / "snap.csv"))
+        assert err.value.status == 5  # MCX_ERR_IO
+        assert "cannot write" in str(err.value)
+
+
 @pytest.mark.parametrize("m", [O.Model(nx=12, ny=10, nz=8, potential="ll"),
                                O.Model(nx=16, ny=16, nz=16, geometry="sphere", potential="ll",
                                        surfaces=[O.Surface("fg", 1.0)]),
