@@ -463,6 +463,32 @@ def test_bulk_and_dead_units_agree_with_direct_pass(pot):
             _assert_same(ref, _run_kernel([d], setup, "march", block, planes))
 
 
+def test_tiles_on_a_periodic_custom_mask():
+    """Tiled units where every axis is periodic: a custom mask active in the
+    slab 4 <= x < 44 of a 48 x 24 x 16 box (homeotropic sites at its two x
+    faces, inactive outside), so every row crosses the mask's edge; the middle
+    tile column and its x neighbours hold only bulk sites, and the tiles' y
+    and z neighbours wrap around.  Bit-identical to the direct pass."""
+    m = O.Model(nx=48, ny=24, nz=16, geometry="custom", potential="ghrl", k11=1.0, k22=0.7, k33=1.3, p0=12,
+                xbound="periodic", ybound="periodic", zbound="periodic", elecA=0.4, elecZ=1.0, elecE=1.0,
+                surfaces=[O.Surface("homeotropic", 2.0)])
+    i = np.arange(m.n) % m.nx
+    pt = np.where((i >= 4) & (i < 44), 1, 0).astype(np.int32)
+    pt[(i == 4) | (i == 43)] = 2
+    ns = np.zeros((m.n, 3), np.float32)
+    ns[i == 4] = (-1, 0, 0)
+    ns[i == 43] = (1, 0, 0)
+    d = desc_from_model(m, T=0.9, seed=17, stream=3)
+
+    def setup(eng):
+        eng.set_mask(0, pt, ns)
+        eng.set_state(0, random_state(m, pt, np.random.default_rng(21)))
+
+    ref = _run_kernel([d], setup, "direct", 0, 0)
+    for block, planes in ((64, 8), (128, 4), (256, 0), (64, -2)):
+        _assert_same(ref, _run_kernel([d], setup, "march", block, planes))
+
+
 LONG_RUNS = {
     # chiral GHRL droplets with planar anchoring in a field: masked units of
     # every kind (surface, bulk, dead)
