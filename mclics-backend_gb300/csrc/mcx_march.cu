@@ -5,7 +5,9 @@
 //            Monte_Carlo_Step, src/evolve.cpp:64-179 of the reference, with 2
 //            colours instead of 8).  A CTA owns NT consecutive same-colour
 //            site pairs of one z-plane (pairs numbered row-major within the
-//            plane) and marches them through a chunk of K planes.  Per plane
+//            plane; in masked replicas whose rows cross the mask's edge, a
+//            tile of kTileW pairs x NT / kTileW rows) and marches them
+//            through a chunk of K planes.  Per plane
 //            a thread loads its own pair (3 float2), the opposite colour's
 //            pair in the same row (its x neighbours), one extra opposite site
 //            (the remaining x neighbour) and the opposite pairs of rows y+1
