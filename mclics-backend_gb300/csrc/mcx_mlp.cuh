@@ -186,12 +186,12 @@ __device__ __forceinline__ void mlp_warp(const uint8_t *W, const __nv_bfloat16 *
 // log cosh, stable: |x| + log(1 + exp(-2|x|)) (the -log 2 cancels in ratios).
 __device__ __forceinline__ float log_cosh_shift(float x) {
   const float a = fabsf(x);
-  return a + log1pf(__expf(-2.f * a));
+  return __fadd_rn(a, log1pf(__expf(__fmul_rn(-2.f, a))));
 }
 
 // The mixture's mean axis and concentration from the network outputs.
 __device__ __forceinline__ void vmf_params(const float y[4], float mu[3], float &kappa) {
-  const float nm2 = y[0] * y[0] + y[1] * y[1] + y[2] * y[2];
+  const float nm2 = fmaf(y[2], y[2], fmaf(y[1], y[1], __fmul_rn(y[0], y[0])));
   if (nm2 > 1e-24f) {
     const float inv = rsqrtf(nm2);
     mu[0] = y[0] * inv;

@@ -568,12 +568,16 @@ __device__ __forceinline__ unsigned site_update_learned(const RepDev &R, const P
       vmf_params(yo, mu, kappa);
       vmf_sample(mu, kappa, u01(r.x), u01(r.y), u01(r.z), v);
       const float b_new = bond_sum<POT>(R, v[0], v[1], v[2], nb, w);
-      float dE = bond_scale<POT>(R) * (b_new - b_old);
+      // every rounding of the log ratio fixed, as for the plain move's dE:
+      // the learned forms with the same network take the same decisions
+      float dE = __fmul_rn(bond_scale<POT>(R), __fsub_rn(b_new, b_old));
       if (surf)
-        dE += surface_energy(R, sid, v[0], v[1], v[2], sx, sy, sz) - surface_energy(R, sid, x, y, z, sx, sy, sz);
-      if (FIELD) dE += field_energy(R, v[0], v[1], v[2]) - field_energy(R, x, y, z);
-      const float lr = -dE * invT + log_cosh_shift(kappa * (mu[0] * x + mu[1] * y + mu[2] * z)) -
-                       log_cosh_shift(kappa * (mu[0] * v[0] + mu[1] * v[1] + mu[2] * v[2]));
+        dE = __fadd_rn(dE, __fsub_rn(surface_energy(R, sid, v[0], v[1], v[2], sx, sy, sz),
+                                     surface_energy(R, sid, x, y, z, sx, sy, sz)));
+      if (FIELD) dE = __fadd_rn(dE, __fsub_rn(field_energy(R, v[0], v[1], v[2]), field_energy(R, x, y, z)));
+      const float lo = log_cosh_shift(__fmul_rn(kappa, dot3_rn(mu[0], mu[1], mu[2], x, y, z)));
+      const float ln = log_cosh_shift(__fmul_rn(kappa, dot3_rn(mu[0], mu[1], mu[2], v[0], v[1], v[2])));
+      const float lr = __fsub_rn(fmaf(-dE, invT, lo), ln);
       const bool accept = u01(r.w) < __expf(lr);
       if (TRACE) {
         a.tr_dE[nat] = dE;

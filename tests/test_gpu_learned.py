@@ -162,18 +162,18 @@ def test_learned_march_equals_learned_direct_pass(name):
 
 def test_learned_forms_agree_over_long_runs():
     """32 chiral droplets in a field, 50 + 50 measured learned sweeps: the
-    learned z-march with the tensor-core network, with the warp-level network,
-    and the learned direct pass part (the tensor-core network sums in another
-    order; decisions within an ulp of their threshold part the other two),
-    but they sample the same states: replica-averaged S and E of each z-march
-    form agree with the direct pass's within 3 combined standard errors."""
+    learned z-march with the warp-level network runs the learned direct
+    pass's chain bit for bit (the same network code, and the MH ratio's
+    roundings fixed); the tensor-core network sums in another order, so its
+    chain parts from theirs, but it samples the same states: replica-averaged
+    S and E agree with the direct pass's within 3 combined standard errors."""
     m = O.Model(nx=64, ny=64, nz=64, geometry="sphere", xbound="free", ybound="free", zbound="free",
                 potential="ghrl", k11=1.0, k22=0.6, k33=1.4, p0=20.0, elecA=1.0, elecZ=1.0, elecE=0.5, radius=26.0,
                 surfaces=[O.Surface("fg", 1.0)])
     R = 32
     descs = [desc_from_model(m, T=0.8, seed=500 + q, stream=q) for q in range(R)]
     params = _weights(4)
-    means = []
+    means, states = [], []
     for kind, path in (("direct", None), ("march", "tcgen05"), ("march", "warp")):
         with mcx.Engine(descs) as eng:
             eng.pass_kind = kind
@@ -187,8 +187,11 @@ def test_learned_forms_agree_over_long_runs():
             eng.reset_stats()
             eng.sweep(50, measure=True)
             st = [eng.stats(q) for q in range(R)]
+            states.append([eng.get_state(q) for q in range(R)])
         means.append((np.array([t[mcx.ST_S1] / t[mcx.ST_N] for t in st]),
                       np.array([t[mcx.ST_E1] / t[mcx.ST_N] for t in st])))
+    for q in range(R):  # warp-level learned z-march == learned direct pass
+        assert np.array_equal(states[0][q], states[2][q]), q
     for other in means[1:]:
         for a, b in zip(means[0], other):
             se = np.sqrt(a.var(ddof=1) / len(a) + b.var(ddof=1) / len(b))
