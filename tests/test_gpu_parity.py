@@ -160,11 +160,14 @@ def test_measure_parity(name):
         assert abs(abs(np.dot(g["director"], o["director"])) - 1) < 1e-5
 
 
-@pytest.mark.parametrize("name", ["bulk_ll", "sphere_ghrl_fg_field", "custom_mixed", "slab_ghrl_padded",
-                                  "sphere_pear_homeotropic", "sphere_ghrl_odd11", "custom_odd", "bulk_pear_odd_x"])
+@pytest.mark.parametrize("name", ["bulk_ll", "bulk_ghrl_field", "sphere_ghrl_fg_field", "custom_mixed",
+                                  "slab_ghrl_padded", "sphere_pear_homeotropic", "sphere_ghrl_odd11", "custom_odd",
+                                  "bulk_pear_odd_x"])
 def test_sweeps_and_step_rule_match_oracle(name):
     """Three measured sweeps through the graph-free path: same states, same
-    step-size sequence, same running sums as the oracle's red/black sweeps."""
+    step-size sequence, same running sums as the oracle's red/black sweeps
+    (for the unmasked cases the colour-1 pass also measures the colour-0
+    sites, with the field term in bulk_ghrl_field)."""
     T, ang, seed, stream = 0.9, 0.5, 5, 1
     m, lat, eng, ni0 = _setup(name, T, seed, stream, ang)
     with eng:
