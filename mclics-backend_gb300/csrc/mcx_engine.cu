@@ -377,7 +377,7 @@ static std::vector<int2> plane_runs(const mcx_engine *e, int r) {
 static bool use_tiles(const mcx_engine *e, int r) {
   const RepDev &R = e->rep[r];
   return e->var.mask && !e->var.odd && !e->pmarch && !e->qmarch && r < (int)e->tiled.size() && e->tiled[r] &&
-         R.hp >= 2 * kTileW && R.hp < (1 << kTileQBits);
+         R.hp >= 2 * kTileW && R.hp < (1 << kTileQBits) && R.ny < (1 << (30 - kTileQBits));  // (j0 << 12) | q0 fits
 }
 
 static void plan_march(mcx_engine *e) {
