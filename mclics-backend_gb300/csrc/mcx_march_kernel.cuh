@@ -95,6 +95,7 @@ __global__ void __launch_bounds__(NT, march_min_blocks<POT, MASK, NT>()) k_march
   float qs[kQ];
 #pragma unroll
   for (int q = 0; q < kQ; q++) qs[q] = 0.f;
+  int slot = -1;  // the sweep's ring slot (measured passes)
   int p = u.y + (int)threadIdx.x;
   bool live = p < R.hp * R.ny;
   if (MASK && (u.w & kUnitTiled)) {  // a tile: kTileW pairs of each of NT / kTileW rows
@@ -111,6 +112,9 @@ __global__ void __launch_bounds__(NT, march_min_blocks<POT, MASK, NT>()) k_march
     // directors may still be written by the previous pass (programmatic
     // dependent launch lets this grid start while that one drains)
     grid_dependency_wait(m);
+    // the ring slot read here, off the CTA's tail (headline lattice +0.8%);
+    // not in the masked field build, where the live register cost it 1.1%
+    if (MODE == MODE_SWEEP_MEASURE && !(MASK && FIELD) && threadIdx.x < kQ) slot = ring_slot(a, S);
     if (MASK && (u.w & kUnitDead))
       dead_unit<FIELD, MODE>(R, m, kb, ke, qs);
     else if (MASK && (u.w & kUnitBulk))  // only bulk sites around: the unmasked update
@@ -120,7 +124,7 @@ __global__ void __launch_bounds__(NT, march_min_blocks<POT, MASK, NT>()) k_march
   }
   grid_dependency_wait();    // threads without a pair reach here without having waited
   grid_launch_dependents();  // the next pass may start its set-up now
-  flush_replica<NT, MODE>(a, r, 1, (unsigned)R.mcta, acc, qs, MASK);
+  flush_replica<NT, MODE>(a, r, 1, (unsigned)R.mcta, acc, qs, MASK, -1, slot);
 }
 
 }  // namespace mcx

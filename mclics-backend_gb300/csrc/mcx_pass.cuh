@@ -233,9 +233,19 @@ __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)_
 // colour: the pass's colour when the kernel runs several passes (a.colour
 // otherwise).  Replica state and running sums are read past L1 (__ldcg): a
 // kernel that runs several passes reads what other CTAs wrote in this launch.
+// The ring slot of the sweep a measured pass adds to.  Only the CTA that
+// ends a replica's colour-1 pass advances S->meas, after every CTA of that
+// pass has added to the slot, so a pass may read it once the previous pass
+// is done (after griddepcontrol.wait).
+__device__ __forceinline__ int ring_slot(const PassArgs &a, const RepState *S) {
+  return (int)(__ldcg(&S->meas) % (unsigned long long)a.ring_cap);
+}
+
+// slot_pre: the ring slot if the caller read it early (ring_slot; -1: read
+// it here, at the end of the CTA, where its latency is exposed).
 template <int NT, int MODE>
 __device__ __forceinline__ void flush_replica(const PassArgs &a, int r, int units, unsigned total, unsigned acc,
-                                              float qs[kQ], bool mask, int colour = -1) {
+                                              float qs[kQ], bool mask, int colour = -1, int slot_pre = -1) {
   constexpr bool MEAS = MODE == MODE_SWEEP_MEASURE || MODE == MODE_MEASURE_ONLY;
   constexpr bool COUNT = MODE == MODE_SWEEP || MODE == MODE_SWEEP_MEASURE;
   __shared__ unsigned s_acc[NT / 32];
@@ -276,6 +286,7 @@ __device__ __forceinline__ void flush_replica(const PassArgs &a, int r, int unit
 #pragma unroll
     for (int w2 = 0; w2 < NT / 32; w2++) v += s_q[w2][q];
     const unsigned long long slot = MODE == MODE_MEASURE_ONLY ? (unsigned long long)a.ring_cap
+                                    : slot_pre >= 0           ? (unsigned long long)slot_pre
                                                               : __ldcg(&S->meas) % (unsigned long long)a.ring_cap;
     double *ring = a.ring + (((size_t)r * (a.ring_cap + 1) + slot) * kLanes + lane_slot) * kQ;
     atomicAdd(ring + threadIdx.x, (double)v);
