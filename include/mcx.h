@@ -215,13 +215,11 @@ mcx_status mcx_set_staged(mcx_engine *eng, int on);
 int mcx_get_staged(const mcx_engine *eng);
 
 /* The kernel that runs the plain proposal's sweeps.  All compute the same
- * update from the same Philox counters, and each is deterministic run to
- * run; two forms agree bit for bit except where a decision lies within an
- * ulp of its threshold (about one in 10^7-10^8 updates: the compiler fuses
- * multiply-adds per kernel), after which their trajectories part but sample
- * the same states.  Pin the form and shape (mcx_set_pass,
- * mcx_set_march_shape) for runs that must repeat bit for bit: the
- * autotuner's choice depends on timing.
+ * update from the same Philox counters with every rounding of the energy
+ * change fixed, so every form and shape runs the same chain bit for bit
+ * (states, step sizes, acceptance counts; the measured sums agree to FP32
+ * summation order): the autotuner's choice changes the speed, never the
+ * trajectory.
  *
  *   MCX_PASS_MARCH   the default: a CTA marches a block of same-colour site
  *                    pairs of one z-plane through a chunk of planes, keeping
