@@ -23,8 +23,8 @@
 // coherent between SMs.  Point types and normals never change and keep the
 // read-only path.  Per pass the work is that of k_march (mcx_march.cu) with
 // the same units, Philox counters and pair update, so results agree with it
-// bit for bit except at decisions within an ulp of their threshold (see
-// mcx_march.cu).
+// bit for bit (the energy change fixes its roundings: bond_sum in
+// mcx_pass.cuh).
 #include <cuda_runtime.h>
 
 #include "mcx_march.cuh"

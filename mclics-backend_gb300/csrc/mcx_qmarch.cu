@@ -15,9 +15,8 @@
 //
 // Same work units (of 2 x threads pairs), Philox counters (pair index
 // row * hp + q, sweep, colour) and pair update (update_pair_draw) as k_march:
-// the two agree bit for bit except at decisions within an ulp of their
-// threshold (the compiler fuses multiply-adds per kernel).  Unmasked batches
-// whose rows hold whole quads (nx a multiple of 8).
+// the two agree bit for bit (the energy change fixes its roundings).
+// Unmasked batches whose rows hold whole quads (nx a multiple of 8).
 #include <cuda_runtime.h>
 
 #include "mcx_march.cuh"

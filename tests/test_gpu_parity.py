@@ -526,10 +526,10 @@ def _assert_same_chain(ref, out, what):
 def test_pass_forms_identical_over_long_runs(name):
     """16 replicas, 100 + 100 measured sweeps (about 10^8 site updates per
     form): every form runs the same chain bit for bit.  The forms inline the
-    same update into different code and the compiler fuses multiply-adds per
-    kernel, so their energy changes can differ in the last bits; a decision
-    that falls within the near-tie band is retaken from the energy change
-    every form computes with the same roundings, so none goes the other way."""
+    same update into different code; left to the compiler, their multiply-add
+    fusions could differ and a decision within an ulp of its threshold could
+    go either way, so the energy change fixes every rounding in the source
+    (bond_sum, site_update) and all forms take the same decisions."""
     m = O.Model(**LONG_RUNS[name])
     descs = [desc_from_model(m, T=0.8 if m.potential != "ll" else 1.12, seed=500 + q, stream=q) for q in range(16)]
 
@@ -560,11 +560,11 @@ def test_pass_forms_identical_over_long_runs(name):
 
 def test_pass_forms_identical_on_droplets_300_sweeps():
     """Chiral droplets in a field (8 replicas of 96^3, r = 40), 300 sweeps:
-    about 7*10^8 active-site updates per form.  Before near ties were
-    decided canonically, the z-march and the direct pass parted on this run
+    about 7*10^8 active-site updates per form.  Before the energy change
+    fixed its roundings, the z-march and the direct pass parted on this run
     within tens of sweeps (a decision within an ulp of its threshold about
-    once per 4*10^7 updates); now the z-march, the four-site march and the
-    direct pass end in the same state."""
+    once per 4*10^7 updates); now the z-march, the four-site march (where it
+    applies) and the direct pass end in the same state."""
     m = O.Model(nx=96, ny=96, nz=96, geometry="sphere", xbound="free", ybound="free", zbound="free",
                 potential="ghrl", k11=1.0, k22=0.6, k33=1.4, p0=20.0, elecA=1.0, elecZ=1.0, elecE=0.5,
                 radius=40.0, surfaces=[O.Surface("fg", 1.0)])
