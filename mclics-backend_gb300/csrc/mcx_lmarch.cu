@@ -116,20 +116,23 @@ __global__ void __launch_bounds__(kLPB, TC ? 3 : MCX_LMARCH_MIN_BLOCKS) k_lmarch
     const bool zp = k + 1 < nz || zper;
     const int up = k + 1 < nz ? 1 : 1 - nz;
     load_opair_at<MASK>(m, m.off + up * m.dz, m.offp + up * m.dzp, zp, op);
+    const int dx = m.s ? m.dx1 : m.dx0;
+    uint16_t pself = 0x0101;
+    if (MASK) pself = __ldg(reinterpret_cast<const uint16_t *>(m.PA + m.offp));
+    // a warp whose 64 sites are all inactive, in an unmeasured sweep: nothing
+    // moves and nothing is measured, so it skips the network and the updates
+    // (the tensor-core form evaluates the network per CTA and does not skip)
+    const bool skip = !TC && MASK && MODE == MODE_SWEEP && __all_sync(0xffffffffu, !valid || pself == 0);
+    if (!skip) {
     float2 ax = *reinterpret_cast<const float2 *>(m.A0 + m.off);
     float2 ay = *reinterpret_cast<const float2 *>(m.A1 + m.off);
     float2 az = *reinterpret_cast<const float2 *>(m.A2 + m.off);
-    const int dx = m.s ? m.dx1 : m.dx0;
     const float exv[3] = {ldo1(m.O0 + m.off + dx), ldo1(m.O1 + m.off + dx), ldo1(m.O2 + m.off + dx)};
     OPair yp, ym;
     load_opair_at<MASK>(m, m.off + m.dyp, m.offp + m.dypp, true, yp);
     load_opair_at<MASK>(m, m.off + m.dym, m.offp + m.dymp, true, ym);
-    uint16_t pself = 0x0101;
     uint8_t pex = 1;
-    if (MASK) {
-      pself = __ldg(reinterpret_cast<const uint16_t *>(m.PA + m.offp));
-      pex = __ldg(m.PO + m.offp + dx);
-    }
+    if (MASK) pex = __ldg(m.PO + m.offp + dx);
     const int s = m.s;
     const float exe = s ? m.ee1 : m.ee0;
     const float erz[4] = {m.eyp, m.eym, zp ? 1.f : 0.f, zm ? 1.f : 0.f};
@@ -227,6 +230,7 @@ __global__ void __launch_bounds__(kLPB, TC ? 3 : MCX_LMARCH_MIN_BLOCKS) k_lmarch
       *reinterpret_cast<float2 *>(m.A1 + m.off) = ay;
       *reinterpret_cast<float2 *>(m.A2 + m.off) = az;
     }
+    }  // !skip
     om = o0;
     o0 = op;
     zm = true;
