@@ -119,10 +119,12 @@ __global__ void __launch_bounds__(kLPB, TC ? 3 : MCX_LMARCH_MIN_BLOCKS) k_lmarch
     const int dx = m.s ? m.dx1 : m.dx0;
     uint16_t pself = 0x0101;
     if (MASK) pself = __ldg(reinterpret_cast<const uint16_t *>(m.PA + m.offp));
-    // a warp whose 64 sites are all inactive, in an unmeasured sweep: nothing
-    // moves and nothing is measured, so it skips the network and the updates
-    // (the tensor-core form evaluates the network per CTA and does not skip)
-    const bool skip = !TC && MASK && MODE == MODE_SWEEP && __all_sync(0xffffffffu, !valid || pself == 0);
+    // a warp whose 64 sites are all inactive: nothing moves, so it needs no
+    // network, and in an unmeasured sweep nothing is measured either, so it
+    // skips the updates too (the tensor-core form evaluates the network per
+    // CTA and does not skip)
+    const bool idle = !TC && MASK && __all_sync(0xffffffffu, !valid || pself == 0);
+    const bool skip = idle && MODE == MODE_SWEEP;
     if (!skip) {
     float2 ax = *reinterpret_cast<const float2 *>(m.A0 + m.off);
     float2 ay = *reinterpret_cast<const float2 *>(m.A1 + m.off);
@@ -185,6 +187,9 @@ __global__ void __launch_bounds__(kLPB, TC ? 3 : MCX_LMARCH_MIN_BLOCKS) k_lmarch
         yA[q] = y[0][q];
         yB[q] = y[1][q];
       }
+    } else if (idle) {  // no active site: the outputs are never read
+#pragma unroll
+      for (int q = 0; q < 4; q++) yA[q] = yB[q] = 0.f;
     } else {
       // the network for the warp's 64 sites
       __syncwarp();
