@@ -102,15 +102,16 @@ def _time_port(side, threads, seconds, q):
 
 
 def test_port_runs_at_the_reference_speed():
-    """Median of three back-to-back rounds, one thread, a 64^3 LL lattice."""
+    """Best of five alternating rounds each, one thread, a 64^3 LL lattice
+    (the best round filters out time the host spent on other work)."""
     ctx = mp.get_context("spawn")
     rates = {"ref": [], "port": []}
-    for _ in range(3):
+    for _ in range(5):
         for key, fn in (("ref", _time_ref), ("port", _time_port)):
             q = ctx.Queue()
             p = ctx.Process(target=fn, args=(64, 1, 1.5, q))
             p.start()
             rates[key].append(q.get(timeout=120))
             p.join()
-    ratio = np.median(rates["port"]) / np.median(rates["ref"])
+    ratio = np.max(rates["port"]) / np.max(rates["ref"])
     assert 0.9 <= ratio <= 1.1, (ratio, rates)
